@@ -1,0 +1,524 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 domain-wall Wilson hopping term (GridBench's Dhop).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--quick]
+
+Headline workload: FP32 Dhop on a 16^4 x Ls=16 periodic lattice with seeded random SU(3)
+links and a Gaussian fermion.  One step = one application of the hopping term to the whole
+lattice (1320 flop per 5D site, GridBench's own count).  Two in/out pairs alternate, so the
+working set (476 MB) is well above the 129 MB L2 between consecutive steps.
+
+The JSON line carries: value (device-timed GFLOP/s, inputs resident in HBM), the HBM
+roofline of the kernel (algorithmic bytes 2*S + 8*G/(Ls*k) per 5D site), e2e (the same
+metric through the public API with the step's input copied from pinned host memory and the
+result copied back every step), the CPU baseline (the oracle port timed on the host cores),
+SM clocks sampled during the timed region, the number of kernels launched, and secondary
+workloads (FP64, DhopDag, FP16 storage, 12-RHS, mixed vs plain CG, batched persistent).
+
+--impl reference times the reference's algorithm on the host CPU (the oracle port of
+dslash_simple.h, all host threads) on the same workload; each step is a bounded sample of
+the lattice.  Multi-GPU (torchrun, N>1) runs independent replicas (the path does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import datetime as _dt
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FLOP_PER_SITE = 1320
+SPINOR_BYTES = {0: 192, 1: 96, 2: 52}  # per 5D site: F64, F32, F16 (+4 B norm)
+LINK_BYTES = {0: 144, 1: 72, 2: 24, 3: 24}  # per link: F64, F32, 12-real F16/BF16
+METRIC = "Dhop GFLOP/s & % HBM roofline; mixed vs plain CG time-to-1e-10 on 1 GB300"
+DIMS = (16, 16, 16, 16)
+LS = 16
+
+
+def algo_bytes(sprec: int, gprec: int, Ls: int, k: int = 1) -> float:
+    """Algorithmic bytes per 5D site per right-hand side: read + write one spinor, links
+    amortised over the Ls*k slices that share them (neighbour table excluded)."""
+    return 2 * SPINOR_BYTES[sprec] + 8 * LINK_BYTES[gprec] / (Ls * k)
+
+
+# ------------------------------------------------------------------ distributed plumbing
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+            if vis and "," in vis:
+                ids = vis.split(",")
+                os.environ["CUDA_VISIBLE_DEVICES"] = ids[self.local % len(ids)]
+            elif not vis:
+                os.environ["CUDA_VISIBLE_DEVICES"] = str(self.local)
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ------------------------------------------------------------------ clocks during the timed region
+class Clocks:
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+        self.t0 = self.t1 = None
+
+    def start(self):
+        if shutil.which("nvidia-smi") is None:
+            return
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or "0"
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        self.proc = subprocess.Popen(["nvidia-smi", "-i", vis, "--query-gpu=" + self.FIELDS,
+                                      "--format=csv,noheader,nounits", "-lms", "100"],
+                                     stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        time.sleep(1.0)  # let the sampler start before the timed region
+
+    def mark(self, which: str):
+        setattr(self, which, _dt.datetime.now())
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 10:
+                continue
+            try:
+                ts = _dt.datetime.strptime(p[0], "%Y/%m/%d %H:%M:%S.%f")
+                rows.append((ts, float(p[2]), float(p[3]), p[6:10]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        inside = [r for r in rows if self.t0 and self.t1 and self.t0 <= r[0] <= self.t1] or rows
+        if not inside:
+            return None
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({names[i] for r in inside for i, v in enumerate(r[3]) if v.lower().startswith("active")})
+        sm = sorted(r[1] for r in inside)
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(r[2] for r in inside), "reasons": reasons,
+                "samples": len(inside)}
+
+
+def measured_peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(key: str):
+    """DRAM bytes per launch from a committed ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(key)
+    except (OSError, ValueError):
+        return None
+
+
+# ------------------------------------------------------------------ our arm
+def cpu_baseline(dims, Ls, budget_s=10.0) -> dict:
+    """The oracle port (scalar C restatement of dslash_simple.h, OpenMP over all host
+    threads) on the full FP32 lattice, repeated for about budget_s seconds."""
+    import gridbench_gb300 as gb
+    import oracle
+    U = gb.generate_gauge(dims).astype(np.float32)
+    phi = gb.generate_fermion(dims, Ls).astype(np.float32)
+    nbr, prm, nsite = gb.generate_table(dims, Ls)
+    out = np.zeros_like(phi)
+    oracle.dslash_sites(U, phi, out, nbr, 0, nsite, Ls)  # warm
+    t = time.perf_counter()
+    oracle.dslash_sites(U, phi, out, nbr, 0, nsite, Ls)
+    one = time.perf_counter() - t
+    reps = max(1, min(1000, int(budget_s / max(one, 1e-6))))
+    t = time.perf_counter()
+    for _ in range(reps):
+        oracle.dslash_sites(U, phi, out, nbr, 0, nsite, Ls)
+    dt = time.perf_counter() - t
+    return {"value": round(FLOP_PER_SITE * nsite * Ls * reps / dt / 1e9, 3), "unit": "GFLOP/s",
+            "cores": oracle.threads(), "kind": "port",
+            "sample": f"{reps} full FP32 Dhop passes over {'x'.join(map(str, dims))} x Ls={Ls} "
+                      f"({dt:.1f} s, oracle port of dslash_simple.h with OpenMP)"}
+
+
+def time_dhop(gb, g, pairs, steps, warmup, dag=0):
+    """Device time (ms) of `steps` hopping applications alternating over (out, in) pairs."""
+    for i in range(warmup):
+        y, x = pairs[i % len(pairs)]
+        gb.dhop(g, y, x, dag)
+    gb.synchronize()
+    t = gb.Timer()
+    n0 = gb.launch_count()
+    t.start()
+    for i in range(steps):
+        y, x = pairs[i % len(pairs)]
+        gb.dhop(g, y, x, dag)
+    ms = t.stop()
+    return ms, gb.launch_count() - n0
+
+
+def rel_to(gb, lat, a, b) -> float:
+    """|a - b| / |b| on the device in FP64."""
+    d = gb.Field(lat, gb.F64)
+    d.copy_from(a)
+    bb = gb.Field(lat, gb.F64)
+    bb.copy_from(b)
+    d.axpby(-1.0, bb, 1.0)
+    return float(np.sqrt(d.norm2() / bb.norm2()))
+
+
+def secondary(gb, args, peak) -> dict:
+    out = {}
+    lat = gb.Lattice.periodic(DIMS, LS)
+    V5 = int(np.prod(DIMS)) * LS
+    g64 = gb.Gauge(lat, None, gb.F64, seed=11)
+    g32 = gb.Gauge(lat, None, gb.F32, seed=11)
+    g16 = gb.Gauge(lat, None, gb.F16, seed=11)
+    x64 = gb.Field(lat, gb.F64).gaussian(21)
+    y64 = gb.Field(lat, gb.F64)
+    x32, y32 = gb.Field(lat, gb.F32), gb.Field(lat, gb.F32)
+    x32.copy_from(x64)
+    x16, y16 = gb.Field(lat, gb.F16), gb.Field(lat, gb.F16)
+    x16.copy_from(x64)
+    steps = 200
+    for name, g, x, y, sp, gp, dag in (("dhop_f64_16^4x16", g64, x64, y64, 0, 0, 0),
+                                       ("dhopdag_f32_16^4x16", g32, x32, y32, 1, 1, 1),
+                                       ("dhop_f16_16^4x16", g16, x16, y16, 2, 2, 0)):
+        gb.tune_dhop(g, y, x, dag)
+        n = steps if sp != 0 else 40
+        ms, _ = time_dhop(gb, g, [(y, x)], n, 5, dag)
+        t = ms / n / 1e3
+        ref = gb.Field(lat, gb.F64)
+        gb.dhop(g64, ref, x64, dag)
+        rec = {"gflops": round(FLOP_PER_SITE * V5 / t / 1e9, 1), "ms": round(t * 1e3, 4),
+               "hbm_frac": round(algo_bytes(sp, gp, LS) * V5 / t / 1e9 / peak, 3),
+               "rel_err_vs_fp64": 0.0 if sp == 0 else rel_to(gb, lat, y, ref),
+               "launch": list(gb.tune_query(g, x))}
+        if sp == 0:
+            rec["fp64_tflops"] = round(FLOP_PER_SITE * V5 / t / 1e12, 3)
+        out[name] = rec
+    del g64, g32, g16, x64, y64, x32, y32, x16, y16, lat
+    if not args.quick:
+        out["multi_rhs_24^4x12_k12"] = bench_mrhs(gb, peak)
+        out["batch_64"] = bench_batch(gb)
+        out["cg_32^4x16"] = bench_cg(gb, args)
+    return out
+
+
+def bench_mrhs(gb, peak) -> dict:
+    dims, Ls, k = (24, 24, 24, 24), 12, 12
+    lat = gb.Lattice.periodic(dims, Ls)
+    V5 = int(np.prod(dims)) * Ls
+    g = gb.Gauge(lat, None, gb.F32, seed=5)
+    X, Y = gb.Field(lat, gb.F32, k), gb.Field(lat, gb.F32, k)
+    for r in range(k):
+        X.gaussian(100 + r, r)
+    gb.tune_dhop(g, Y, X)
+    ms_multi, _ = time_dhop(gb, g, [(Y, X)], 10, 2)
+    t_multi = ms_multi / 10 / 1e3
+    x1, y1 = gb.Field(lat, gb.F32), gb.Field(lat, gb.F32)
+    gb.tune_dhop(g, y1, x1)
+    # 12 single-RHS launches per step
+    singles = []
+    for r in range(k):
+        s = gb.Field(lat, gb.F32)
+        s.gaussian(100 + r, 0)
+        singles.append(s)
+    outs = [gb.Field(lat, gb.F32) for _ in range(2)]
+    ms_single, _ = time_dhop(gb, g, [(outs[r % 2], singles[r]) for r in range(k)], 10 * k, k)
+    t_single = ms_single / 10 / 1e3
+    # error of the 12-RHS result against single launches (rhs 0), through host export
+    gb.dhop(g, Y, X)
+    gb.dhop(g, y1, singles[0])
+    err = float(np.linalg.norm(Y.numpy(0) - y1.numpy()) / np.linalg.norm(y1.numpy()))
+    per_src_multi = FLOP_PER_SITE * V5 * k / t_multi / 1e9
+    per_src_single = FLOP_PER_SITE * V5 * k / t_single / 1e9
+    return {"gflops_12rhs": round(per_src_multi, 1), "gflops_12x1rhs": round(per_src_single, 1),
+            "per_source_speedup": round(per_src_multi / per_src_single, 3),
+            "byte_model_ceiling": round(algo_bytes(1, 1, Ls, 1) / algo_bytes(1, 1, Ls, k), 3),
+            "hbm_frac_12rhs": round(algo_bytes(1, 1, Ls, k) * V5 * k / t_multi / 1e9 / peak, 3),
+            "rel_err_vs_single": err, "launch": list(gb.tune_query(g, X))}
+
+
+def bench_batch(gb) -> dict:
+    rng = np.random.default_rng(2024)
+    vols = [8, 12, 16, 20, 24]
+    keep, G, O, I = [], [], [], []
+    flops = 0
+    sites5 = 0
+    for k in range(64):
+        L = int(rng.choice(vols))
+        Ls = int(rng.choice([8, 12, 16]))
+        prec = gb.F32 if rng.random() < 0.5 else gb.F16
+        lat = gb.Lattice.periodic((L, L, L, L), Ls)
+        g = gb.Gauge(lat, None, prec, seed=1000 + k)
+        x = gb.Field(lat, prec).gaussian(2000 + k)
+        y = gb.Field(lat, prec)
+        keep.append(lat)
+        G.append(g)
+        O.append(y)
+        I.append(x)
+        flops += FLOP_PER_SITE * L ** 4 * Ls
+        sites5 += L ** 4 * Ls
+    t0 = time.perf_counter()
+    b = gb.Batch(G, O, I)
+    tune_s = time.perf_counter() - t0
+    for _ in range(3):
+        b.run()
+    gb.synchronize()
+    t = gb.Timer()
+    reps = 10
+    t.start()
+    for _ in range(reps):
+        b.run()
+    ms = t.stop() / reps
+    # the same instances as 64 separate (tuned) launches
+    for g, y, x in zip(G, O, I):
+        gb.dhop(g, y, x)
+    gb.synchronize()
+    t.start()
+    for _ in range(reps):
+        for g, y, x in zip(G, O, I):
+            gb.dhop(g, y, x)
+    ms_sep = t.stop() / reps
+    info = b.info()
+    return {"instances": 64, "sites5": sites5, "gflops": round(flops / (ms / 1e3) / 1e9, 1),
+            "ms_per_replay": round(ms, 3), "ms_64_separate_launches": round(ms_sep, 3),
+            "graph": info["graph"], "ctas": info["ctas"], "threads": info["threads"],
+            "tune_seconds": round(tune_s, 2)}
+
+
+def bench_cg(gb, args) -> dict:
+    dims, Ls = ((32, 32, 32, 32), 16) if not args.cg_small else ((16, 16, 16, 16), 16)
+    M5, mf = 1.8, 0.01
+    lat = gb.Lattice.periodic(dims, Ls)
+    g64 = gb.Gauge(lat, None, gb.F64, seed=77)
+    g32 = gb.Gauge(lat, None, gb.F32, seed=77)
+    g16 = gb.Gauge(lat, None, gb.F16, seed=77)
+    b = gb.Field(lat, gb.F64).gaussian(78)
+    res = {"lattice": f"{'x'.join(map(str, dims))} x Ls={Ls}", "M5": M5, "mf": mf, "tol": 1e-10}
+    for name, mode, gs, sp in (("plain_fp32_fp64res", gb.CG_PLAIN, None, gb.F32),
+                               ("mixed_fp16", gb.CG_MIXED, g16, gb.F16),
+                               ("mixed_fp32", gb.CG_MIXED, g32, gb.F32)):
+        x = gb.Field(lat, gb.F64)
+        try:
+            st = gb.cg_solve(g64, x, b, M5, mf, mode, tol=1e-10, max_iter=args.cg_max_iter, delta=0.1, g32=g32,
+                             gsloppy=gs, sloppy_prec=sp)
+            res[name] = {k: (round(v, 6) if isinstance(v, float) else v) for k, v in st.items()}
+            res[name]["true_residual"] = st["true_residual"]
+        except gb.GbdwError as e:
+            res[name] = {"error": str(e)}
+        del x
+    if "seconds" in res.get("plain_fp32_fp64res", {}) and "seconds" in res.get("mixed_fp16", {}):
+        res["speedup_mixed_fp16_vs_plain"] = round(res["plain_fp32_fp64res"]["seconds"] /
+                                                   res["mixed_fp16"]["seconds"], 3)
+    return res
+
+
+def run_ours(args, D: Dist) -> dict | None:
+    import gridbench_gb300 as gb
+    gb.load()
+    if not gb.device_available():
+        raise SystemExit("bench.py: no CUDA device visible (" + gb.load().gbdw_last_error().decode() + ")")
+    peak, peak_src = measured_peak_hbm()
+    V5 = int(np.prod(DIMS)) * LS
+    lat = gb.Lattice.periodic(DIMS, LS)
+    U = gb.generate_gauge(DIMS)
+    g = gb.Gauge(lat, U, gb.F32)
+    phiA = gb.generate_fermion(DIMS, LS)
+    xA = gb.Field(lat, gb.F32).load(phiA)
+    xB = gb.Field(lat, gb.F32).load(gb.generate_fermion(DIMS, LS, 1, (9, 10, 11, 12)))
+    yA, yB = gb.Field(lat, gb.F32), gb.Field(lat, gb.F32)
+    cfg = gb.tune_dhop(g, yA, xA)
+    pairs = [(yA, xA), (yB, xB)]
+    clocks = Clocks()
+    clocks.start()
+    for i in range(args.warmup):
+        y, x = pairs[i % 2]
+        gb.dhop(g, y, x)
+    gb.synchronize()
+    D.barrier()
+    clocks.mark("t0")
+    ms, launches = time_dhop(gb, g, pairs, args.steps, 0)
+    clocks.mark("t1")
+    clk = clocks.stop()
+    ms = D.max(ms)
+    t_step = ms / args.steps / 1e3
+    flops_step = FLOP_PER_SITE * V5
+    value = D.world * flops_step / t_step / 1e9
+    bytes_launch = algo_bytes(1, 1, LS) * V5
+    achieved = bytes_launch / t_step / 1e9
+    traffic = ncu_traffic("dhop_f32_16^4x16")
+
+    # end to end through the public API: pinned host input -> device -> Dhop -> pinned host output
+    n = V5 * 24
+    hin = gb.PinnedArray(n, np.float32)
+    hin.array[:] = phiA
+    hout = gb.PinnedArray(n, np.float32)
+    e2e_steps = max(3, min(args.steps, 100))
+    for _ in range(2):
+        xA.load(hin.array)
+        gb.dhop(g, yA, xA)
+        yA.export_into(hout.array)
+    D.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        xA.load(hin.array)
+        gb.dhop(g, yA, xA)
+        yA.export_into(hout.array)
+    gb.synchronize()
+    te = D.max(time.perf_counter() - t0) / e2e_steps
+    e2e = {"value": round(D.world * flops_step / te / 1e9, 2), "unit": "GFLOP/s",
+           "h2d_bytes_per_step": int(hin.array.nbytes), "d2h_bytes_per_step": int(hout.array.nbytes),
+           "steps": e2e_steps, "ms_per_step": round(te * 1e3, 4),
+           "path": "Field.load(pinned FP32 reference layout) -> dhop -> Field.export_into(pinned)"}
+
+    # relative error of this FP32 result against the FP64 kernel on the same input
+    g64 = gb.Gauge(lat, U, gb.F64)
+    x64, y64 = gb.Field(lat, gb.F64).load(phiA), gb.Field(lat, gb.F64)
+    gb.dhop(g64, y64, x64)
+    gb.dhop(g, yA, xA)
+    rel = rel_to(gb, lat, yA, y64)
+    del g64, x64, y64
+
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": "GFLOP/s", "n_gpus": D.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 5), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic: seeded random SU(3) links (Gaussian -> Gram-Schmidt -> det 1), N(0,1) fermion",
+        "config": {"workload": "FP32 domain-wall Wilson Dhop, 16^4 x Ls=16, periodic", "lattice": list(DIMS),
+                   "Ls": LS, "parallelism": "replicas" if D.world > 1 else "single",
+                   "l2": "inputs larger than L2: two alternating in/out pairs, 476 MB vs 129 MB L2",
+                   "launch": {"threads": cfg[0], "slices_per_thread": cfg[1]}},
+        "rel_err_vs_fp64": rel,
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
+                     else "fallback 6.8 TB/s",
+                     "algorithmic_bytes_per_launch": int(bytes_launch),
+                     "bytes_per_site": algo_bytes(1, 1, LS)},
+        "e2e": e2e,
+        "clocks": clk,
+        "gpu_launches": int(launches),
+    }
+    if D.rank == 0 and D.world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(DIMS, LS, args.cpu_seconds)
+    if not args.no_secondary:
+        line["secondary"] = secondary(gb, args, peak)
+    return line if D.rank == 0 else None
+
+
+# ------------------------------------------------------------------ reference arm
+def run_reference(args, D: Dist) -> dict | None:
+    """The reference's algorithm on the host CPU: the oracle port of dslash_simple.h (the
+    reference's own kernels are x86-only and its tree is not present on the GPU host), all
+    host threads, each step a bounded sample of the 16^4 x Ls=16 FP32 workload."""
+    if D.rank != 0:
+        return None
+    import gridbench_gb300 as gb
+    import oracle
+    U = gb.generate_gauge(DIMS).astype(np.float32)
+    phi = gb.generate_fermion(DIMS, LS).astype(np.float32)
+    nbr, prm, nsite = gb.generate_table(DIMS, LS)
+    out = np.zeros_like(phi)
+    oracle.dslash_sites(U, phi, out, nbr, 0, nsite, LS)
+    t = time.perf_counter()
+    oracle.dslash_sites(U, phi, out, nbr, 0, nsite, LS)
+    t_full = time.perf_counter() - t
+    budget = args.ref_seconds
+    per_step = budget / max(1, args.steps + args.warmup)
+    frac = min(1.0, per_step / t_full)
+    sample = max(64, int(nsite * frac))
+    sample = min(sample, nsite)
+    for i in range(args.warmup):
+        oracle.dslash_sites(U, phi, out, nbr, 0, sample, LS)
+    t = time.perf_counter()
+    for i in range(args.steps):
+        s0 = (i * sample) % (nsite - sample + 1)
+        oracle.dslash_sites(U, phi, out, nbr, s0, s0 + sample, LS)
+    dt = time.perf_counter() - t
+    value = FLOP_PER_SITE * sample * LS * args.steps / dt / 1e9
+    desc = (f"each step: {sample} of {nsite} 4D sites (x Ls={LS}) of the 16^4 FP32 lattice, "
+            f"{args.steps} steps in {dt:.2f} s")
+    return {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GFLOP/s", "n_gpus": D.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic: seeded random SU(3) links, N(0,1) fermion",
+            "config": {"workload": "FP32 domain-wall Wilson Dhop, 16^4 x Ls=16, periodic", "lattice": list(DIMS),
+                       "Ls": LS, "l2": "host CPU run"},
+            "cpu_baseline": {"value": round(value, 3), "unit": "GFLOP/s", "cores": oracle.threads(), "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": round(value, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20000)
+    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--quick", action="store_true", help="skip the 12-RHS, batch and CG secondaries")
+    ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ref-seconds", type=float, default=30.0)
+    ap.add_argument("--cg-small", action="store_true", help="CG secondary on 16^4 x 16 instead of 32^4 x 16")
+    ap.add_argument("--cg-max-iter", type=int, default=20000)
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    D = Dist()
+    try:
+        line = run_reference(args, D) if args.impl == "reference" else run_ours(args, D)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+    finally:
+        D.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,335 @@
+"""GB300-native domain-wall Wilson hopping term (GridBench's Dhop) -- Python host mirror.
+
+Everything here forwards to libgbdw.so through its C ABI (include/gbdw.h); numpy arrays
+carry host data in GridBench's reference layout.  The names follow the reference:
+dslash_kernel() is the seam of WilsonKernelsHand.h:17-29, generate_*() play the role of
+TableGenerate.cc, and the objects (Lattice, Gauge, Field) expose the GB300 layout.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Sequence
+
+import numpy as np
+
+from . import _native
+from ._native import (BF16, CG_DOUBLE, CG_MIXED, CG_PLAIN, F16, F32, F64, CGParams, CGStats, GbdwError,
+                      check, load)
+
+__all__ = ["F64", "F32", "F16", "BF16", "CG_PLAIN", "CG_MIXED", "CG_DOUBLE", "GbdwError", "load",
+           "device_available", "launch_count", "synchronize", "seed_from_ints", "generate_gauge",
+           "generate_fermion", "generate_table", "Lattice", "Gauge", "Field", "dhop", "dwf_m", "dwf_mdagm",
+           "cg_solve", "Batch", "dslash_kernel", "Timer", "flush_l2"]
+
+_DT = {F64: np.float64, F32: np.float32}
+
+
+def _ptr(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data)
+
+
+def device_available() -> bool:
+    return bool(load().gbdw_device_available())
+
+
+def launch_count() -> int:
+    return int(load().gbdw_launch_count())
+
+
+def synchronize() -> None:
+    check(load().gbdw_synchronize())
+
+
+def flush_l2(nbytes: int) -> None:
+    check(load().gbdw_flush_l2(nbytes))
+
+
+def seed_from_ints(seeds: Sequence[int]) -> int:
+    a = np.ascontiguousarray(seeds, dtype=np.int32)
+    return int(load().gbdw_seed_from_ints(_ptr(a), len(a)))
+
+
+def _dims(dims) -> np.ndarray:
+    d = np.ascontiguousarray(dims, dtype=np.int32)
+    if d.shape != (4,):
+        raise ValueError("dims must have 4 entries (Lx, Ly, Lz, Lt)")
+    return d
+
+
+def generate_gauge(dims, nsimd: int = 1, seeds=(1, 2, 3, 4)) -> np.ndarray:
+    """Doubled random SU(3) field, reference layout, FP64 (TableGenerate.cc:44,54)."""
+    d = _dims(dims)
+    V = int(np.prod(d))
+    U = np.empty(V * 8 * 9 * 2, dtype=np.float64)
+    check(load().gbdw_generate_gauge(_ptr(d), nsimd, seed_from_ints(seeds), _ptr(U)))
+    return U
+
+
+def generate_fermion(dims, Ls: int, nsimd: int = 1, seeds=(5, 6, 7, 8)) -> np.ndarray:
+    """Gaussian 5D fermion, reference layout, FP64 (TableGenerate.cc:36)."""
+    d = _dims(dims)
+    V = int(np.prod(d))
+    phi = np.empty(V * Ls * 24, dtype=np.float64)
+    check(load().gbdw_generate_fermion(_ptr(d), Ls, nsimd, seed_from_ints(seeds), _ptr(phi)))
+    return phi
+
+
+def generate_table(dims, Ls: int, nsimd: int = 1):
+    """nbr/prm stencil tables (TableGenerate.cc:75-91); returns (nbr uint64, prm uint8, nsite)."""
+    d = _dims(dims)
+    nsite = int(np.prod(d)) // nsimd
+    nbr = np.empty(nsite * Ls * 8, dtype=np.uint64)
+    prm = np.empty(nsite * Ls * 8, dtype=np.uint8)
+    check(load().gbdw_generate_table(_ptr(d), Ls, nsimd, _ptr(nbr), _ptr(prm)))
+    return nbr, prm, nsite
+
+
+class _Handle:
+    _destroy = ""
+
+    def __init__(self):
+        self.h = C.c_void_p()
+
+    def close(self):
+        if self.h and self.h.value:
+            getattr(load(), self._destroy)(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Lattice(_Handle):
+    _destroy = "gbdw_lattice_destroy"
+
+    @classmethod
+    def from_table(cls, nbr: np.ndarray, prm: np.ndarray | None, nsite: int, Ls: int, nsimd: int = 1):
+        self = cls()
+        nbr = np.ascontiguousarray(nbr, dtype=np.uint64)
+        prm_p = None
+        if prm is not None:
+            prm = np.ascontiguousarray(prm, dtype=np.uint8)
+            prm_p = _ptr(prm)
+        check(load().gbdw_lattice_from_table(C.byref(self.h), nsite, Ls, nsimd, _ptr(nbr), prm_p))
+        return self
+
+    @classmethod
+    def periodic(cls, dims, Ls: int):
+        self = cls()
+        d = _dims(dims)
+        check(load().gbdw_lattice_create(C.byref(self.h), _ptr(d), Ls))
+        return self
+
+    def info(self) -> dict:
+        a = (C.c_int64 * 4)()
+        check(load().gbdw_lattice_info(self.h, a))
+        return {"sites": a[0], "Ls": a[1], "nsimd": a[2], "fast": bool(a[3])}
+
+
+class Gauge(_Handle):
+    _destroy = "gbdw_gauge_destroy"
+
+    def __init__(self, lat: Lattice, U: np.ndarray | None, prec: int = F32, seed: int | None = None):
+        """From a reference-layout doubled field U, or (U=None) a device-generated random
+        SU(3) field with the given seed (periodic lattices)."""
+        super().__init__()
+        self.lat = lat
+        self.prec = prec
+        if U is None:
+            check(load().gbdw_gauge_random(C.byref(self.h), lat.h, prec, int(seed or 0)))
+            return
+        U = np.ascontiguousarray(U)
+        src = F64 if U.dtype == np.float64 else F32
+        check(load().gbdw_gauge_create(C.byref(self.h), lat.h, prec, _ptr(U), src))
+
+
+class Field(_Handle):
+    _destroy = "gbdw_field_destroy"
+
+    def __init__(self, lat: Lattice, prec: int = F32, nrhs: int = 1):
+        super().__init__()
+        self.lat = lat
+        self.prec = prec
+        self.nrhs = nrhs
+        check(load().gbdw_field_create(C.byref(self.h), lat.h, prec, nrhs))
+
+    def load(self, phi: np.ndarray, rhs: int = 0) -> "Field":
+        phi = np.ascontiguousarray(phi)
+        src = F64 if phi.dtype == np.float64 else F32
+        check(load().gbdw_field_import(self.h, rhs, _ptr(phi), src))
+        return self
+
+    def numpy(self, rhs: int = 0, dtype=np.float64) -> np.ndarray:
+        info = self.lat.info()
+        n = info["sites"] * info["Ls"] * 24
+        out = np.empty(n, dtype=dtype)
+        check(load().gbdw_field_export(self.h, rhs, _ptr(out), F64 if dtype == np.float64 else F32))
+        return out
+
+    def export_into(self, out: np.ndarray, rhs: int = 0) -> np.ndarray:
+        """Writes right-hand side rhs into a preallocated float64/float32 array (e.g. pinned)."""
+        check(load().gbdw_field_export(self.h, rhs, _ptr(out), F64 if out.dtype == np.float64 else F32))
+        return out
+
+    def gaussian(self, seed: int, rhs: int = 0) -> "Field":
+        check(load().gbdw_field_gaussian(self.h, rhs, int(seed)))
+        return self
+
+    def zero(self):
+        check(load().gbdw_field_zero(self.h))
+
+    def copy_from(self, other: "Field"):
+        check(load().gbdw_field_copy(self.h, other.h))
+
+    def norm2(self) -> float:
+        v = C.c_double()
+        check(load().gbdw_norm2(self.h, C.byref(v)))
+        return v.value
+
+    def dot(self, other: "Field") -> complex:
+        re, im = C.c_double(), C.c_double()
+        check(load().gbdw_dot(self.h, other.h, C.byref(re), C.byref(im)))
+        return complex(re.value, im.value)
+
+    def axpby(self, a: float, x: "Field", b: float):
+        """self = a x + b self"""
+        check(load().gbdw_axpby(a, x.h, b, self.h))
+
+
+def dhop(g: Gauge, out: Field, inp: Field, dag: int = 0) -> None:
+    check(load().gbdw_dhop(g.h, out.h, inp.h, int(dag)))
+
+
+def dwf_m(g: Gauge, out: Field, inp: Field, M5: float, mf: float, dag: int = 0, want_norm: bool = False):
+    v = C.c_double()
+    check(load().gbdw_dwf_m(g.h, out.h, inp.h, M5, mf, int(dag), C.byref(v) if want_norm else None))
+    return v.value if want_norm else None
+
+
+def dwf_mdagm(g: Gauge, out: Field, tmp: Field, inp: Field, M5: float, mf: float) -> float:
+    v = C.c_double()
+    check(load().gbdw_dwf_mdagm(g.h, out.h, tmp.h, inp.h, M5, mf, C.byref(v)))
+    return v.value
+
+
+def cg_solve(g64: Gauge, x: Field, b: Field, M5: float, mf: float, mode: int, tol: float = 1e-10,
+             max_iter: int = 20000, delta: float = 0.1, g32: Gauge | None = None, gsloppy: Gauge | None = None,
+             sloppy_prec: int = F16) -> dict:
+    prm = CGParams(tol, max_iter, delta, sloppy_prec, gsloppy.prec if gsloppy is not None else F16)
+    st = CGStats()
+    status = load().gbdw_cg_solve(g64.h, g32.h if g32 is not None else None,
+                                  gsloppy.h if gsloppy is not None else None, x.h, b.h, M5, mf, mode,
+                                  C.byref(prm), C.byref(st))
+    check(status)
+    return {"iterations": st.iterations, "reliable_updates": st.reliable_updates,
+            "true_residual": st.true_residual, "seconds": st.seconds, "final_rr": st.final_rr}
+
+
+class Batch(_Handle):
+    _destroy = "gbdw_batch_destroy"
+
+    def __init__(self, gauges: Sequence[Gauge], outs: Sequence[Field], ins: Sequence[Field], dag: int = 0):
+        super().__init__()
+        n = len(gauges)
+        self._keep = (list(gauges), list(outs), list(ins))
+        G = (C.c_void_p * n)(*[g.h.value for g in gauges])
+        O = (C.c_void_p * n)(*[o.h.value for o in outs])
+        I = (C.c_void_p * n)(*[i.h.value for i in ins])
+        check(load().gbdw_batch_create(C.byref(self.h), n, G, O, I, int(dag)))
+
+    def run(self):
+        check(load().gbdw_batch_run(self.h))
+
+    def info(self) -> dict:
+        a = (C.c_int64 * 4)()
+        check(load().gbdw_batch_info(self.h, a))
+        return {"items": a[0], "ctas": a[1], "threads": a[2], "graph": bool(a[3])}
+
+
+def tune_dhop(g: Gauge, out: Field, inp: Field, dag: int = 0) -> tuple:
+    check(load().gbdw_tune_dhop(g.h, out.h, inp.h, int(dag)))
+    return tune_query(g, inp)
+
+
+def tune_query(g: Gauge, inp: Field) -> tuple:
+    cfg = (C.c_int * 2)()
+    check(load().gbdw_tune_query(g.h, inp.h, cfg))
+    return int(cfg[0]), int(cfg[1])
+
+
+def tune_set(g: Gauge, inp: Field, threads: int, spt: int):
+    check(load().gbdw_tune_set(g.h, inp.h, threads, spt))
+
+
+def tune_save(path: str):
+    check(load().gbdw_tune_save(path.encode()))
+
+
+def tune_load(path: str):
+    check(load().gbdw_tune_load(path.encode()))
+
+
+class PinnedArray:
+    """numpy view of page-locked host memory (freed with the object)."""
+
+    def __init__(self, n: int, dtype=np.float32):
+        self.ptr = C.c_void_p()
+        nbytes = int(n) * np.dtype(dtype).itemsize
+        check(load().gbdw_host_alloc(nbytes, C.byref(self.ptr)))
+        buf = (C.c_char * nbytes).from_address(self.ptr.value)
+        self.array = np.frombuffer(buf, dtype=dtype, count=int(n))
+
+    def close(self):
+        if self.ptr and self.ptr.value:
+            self.array = None
+            load().gbdw_host_free(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Timer(_Handle):
+    """CUDA-event timer on the library stream."""
+    _destroy = "gbdw_timer_destroy"
+
+    def __init__(self):
+        super().__init__()
+        check(load().gbdw_timer_create(C.byref(self.h)))
+
+    def start(self):
+        check(load().gbdw_timer_start(self.h))
+
+    def stop(self) -> float:
+        ms = C.c_double()
+        check(load().gbdw_timer_stop(self.h, C.byref(ms)))
+        return ms.value
+
+
+def dslash_kernel(nrep: int, U: np.ndarray, out: np.ndarray, inp: np.ndarray, nbr: np.ndarray, nsite: int, Ls: int,
+                  prm: np.ndarray | None, nsimd: int = 1, dag: int = 0) -> float:
+    """The reference seam dslash_kernel(nrep, U, out, in, nbr, nsite, Ls, prm)
+    (WilsonKernelsHand.h:17-29): applies the hopping term nrep times on the GPU and writes
+    `out`; returns microseconds over repetitions 1..nrep-1.  Precision follows the arrays
+    (float64 -> vComplexD, float32 -> vComplexF)."""
+    if not (U.dtype == out.dtype == inp.dtype) or U.dtype not in (np.float64, np.float32):
+        raise TypeError("U, out and in must share dtype float64 or float32")
+    for a in (U, out, inp):
+        if not a.flags.c_contiguous:
+            raise ValueError("arrays must be C-contiguous")
+    prec = F64 if U.dtype == np.float64 else F32
+    nbr = np.ascontiguousarray(nbr, dtype=np.uint64)
+    prm_p = None
+    if prm is not None:
+        prm = np.ascontiguousarray(prm, dtype=np.uint8)
+        prm_p = _ptr(prm)
+    usec = C.c_double()
+    check(load().gbdw_dslash_kernel(nrep, prec, nsimd, _ptr(U), _ptr(out), _ptr(inp), _ptr(nbr), nsite, Ls, prm_p,
+                                    int(dag), C.byref(usec)))
+    return usec.value

@@ -1,0 +1,177 @@
+// Internal types shared by the libgbdw translation units.
+//
+// Device layout ("GB300 layout"), chosen so that consecutive threads read consecutive
+// addresses and one 4D link serves every fifth-dimension slice of its site:
+//   spinor  [site][sc = spin*3+colour][e = s*nrhs + rhs]   complex (F64 16 B, F32 8 B, F16 4 B)
+//           F16 adds norm[site][e] (FP32, max |re|,|im| over the 24 reals of that 5D site)
+//   gauge   [site][mu][row][col] complex, 9 entries (F64/F32) or rows 0-1 only (F16/BF16)
+//   nbr4    [site][mu] uint32 neighbour 4D site (fast path)
+// "site" runs over 4D sites with SIMD lanes unrolled: site = outer_site*nsimd + lane, so a
+// reference table with lane permutes maps onto a plain 4D table.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/gbdw.h"
+
+namespace gbdw {
+
+void set_error(const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+cudaStream_t stream();
+void count_launch(uint64_t n = 1);
+// Device scratch owned by the library (grown on demand, kept until exit).
+void* scratch(size_t bytes, int slot);
+int ensure_device();
+int num_sms();
+
+#define GBDW_CUDA(call)                                       \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return ::gbdw::cuda_fail(e_, #call); \
+  } while (0)
+
+#define GBDW_LAUNCHED()                                                  \
+  do {                                                                   \
+    cudaError_t e_ = cudaGetLastError();                                 \
+    if (e_ != cudaSuccess) return ::gbdw::cuda_fail(e_, "kernel launch"); \
+    ::gbdw::count_launch();                                              \
+  } while (0)
+
+}  // namespace gbdw
+
+struct gbdw_lattice {
+  int64_t nsite;     // 4D sites, lanes unrolled
+  int Ls;
+  int nsimd;
+  int dims[4];       // 0 when built from a table
+  bool fast;         // 4D factorised table available
+  uint32_t* nbr4;    // [nsite][8] (fast)
+  uint32_t* nbr5;    // [nsite][Ls][8] neighbour (site*Ls+s) in device numbering (general)
+};
+
+struct gbdw_gauge {
+  const gbdw_lattice* lat;
+  int prec;
+  void* d;           // device storage
+  size_t bytes;
+};
+
+struct gbdw_field {
+  const gbdw_lattice* lat;
+  int prec;
+  int nrhs;
+  int LsE;           // Ls * nrhs, the innermost extent
+  void* d;           // complex data
+  float* norm;       // F16 only
+  size_t bytes;
+  int64_t elems() const { return lat->nsite * 12 * int64_t(LsE); }  // complex entries
+};
+
+namespace gbdw {
+
+inline size_t spinor_elem_bytes(int prec) { return prec == GBDW_F64 ? 16 : prec == GBDW_F32 ? 8 : 4; }
+inline size_t link_bytes(int prec) {
+  return prec == GBDW_F64 ? 144 : prec == GBDW_F32 ? 72 : 24;
+}
+
+// ------------------------------------------------------------------ small complex helpers
+template <class T>
+struct cpx {
+  T r, i;
+};
+
+template <class T>
+__device__ __forceinline__ cpx<T> cmul(cpx<T> a, cpx<T> b) {
+  return {a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r};
+}
+// acc += a*b
+template <class T>
+__device__ __forceinline__ void cmac(cpx<T>& acc, cpx<T> a, cpx<T> b) {
+  acc.r = fma(a.r, b.r, acc.r);
+  acc.r = fma(-a.i, b.i, acc.r);
+  acc.i = fma(a.r, b.i, acc.i);
+  acc.i = fma(a.i, b.r, acc.i);
+}
+// Multiply by a compile-time unit c in {+1, -1, +i, -i}: code 0:+1 1:-1 2:+i 3:-i
+template <int C, class T>
+__device__ __forceinline__ cpx<T> cunit(cpx<T> a) {
+  if (C == 0) return a;
+  if (C == 1) return {-a.r, -a.i};
+  if (C == 2) return {-a.i, a.r};
+  return {a.i, -a.r};
+}
+template <int C>
+struct conj_unit {
+  static constexpr int v = (C == 2) ? 3 : (C == 3) ? 2 : C;
+};
+
+// ------------------------------------------------------------------ device reductions
+// Block-wide sum followed by a "last block finishes" pass over the per-block partials, so
+// the sum order is fixed (deterministic) and no second launch is needed.  partials holds
+// gridDim.x * W doubles, counter one unsigned that must be zero on entry and is left zero.
+template <int W>
+__device__ __forceinline__ void grid_sum(double (&v)[W], double* partials, unsigned* counter,
+                                         double* result) {
+  __shared__ double sh[32][W];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    double x = v[w];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[warp][w] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      double x = 0.0;
+      for (int k = 0; k < nw; ++k) x += sh[k][w];
+      partials[size_t(blockIdx.x) * W + w] = x;
+    }
+    __threadfence();
+    const unsigned prev = atomicAdd(counter, 1u);
+    last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    double x = 0.0;
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+      x += __ldcg(&partials[size_t(b) * W + w]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[warp][w] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      double x = 0.0;
+      for (int k = 0; k < nw; ++k) x += sh[k][w];
+      result[w] = x;
+    }
+    *counter = 0u;
+  }
+}
+
+// Scratch slots used for reductions: partial sums and a counter/result block.
+struct Reduce {
+  double* partials;
+  unsigned* counter;
+  double* result;
+};
+int reduce_scratch(int64_t nblocks, int width, Reduce* r);
+int reduce_fetch(const Reduce& r, int width, double* host);
+
+}  // namespace gbdw

@@ -1,0 +1,209 @@
+// Process-wide state of libgbdw: last error, the library stream, launch counter, device
+// scratch, timers and the L2 flush.  One host thread drives the library at a time, as the
+// reference's drivers do (bench.cc:59-202); every call is ordered on one CUDA stream.
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <atomic>
+
+#include "common.cuh"
+
+namespace gbdw {
+
+namespace {
+thread_local std::string g_error;
+std::atomic<uint64_t> g_launches{0};
+cudaStream_t g_user_stream = nullptr;
+cudaStream_t g_own_stream = nullptr;
+bool g_have_user_stream = false;
+int g_device_checked = 0;  // 0 unknown, 1 ok, -1 none
+int g_num_sms = 0;
+
+struct ScratchSlot {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+ScratchSlot g_scratch[8];
+double* g_pinned = nullptr;
+}  // namespace
+
+void set_error(const std::string& msg) { g_error = msg; }
+
+int cuda_fail(cudaError_t e, const char* what) {
+  char buf[512];
+  snprintf(buf, sizeof buf, "CUDA error in %s: %s", what, cudaGetErrorString(e));
+  g_error = buf;
+  if (e == cudaErrorMemoryAllocation) return GBDW_ERR_ALLOC;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return GBDW_ERR_NO_DEVICE;
+  return GBDW_ERR_CUDA;
+}
+
+int ensure_device() {
+  if (g_device_checked == 1) return GBDW_OK;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    g_device_checked = -1;
+    set_error("no CUDA device available: libgbdw has no CPU fallback");
+    return GBDW_ERR_NO_DEVICE;
+  }
+  int dev = 0;
+  GBDW_CUDA(cudaGetDevice(&dev));
+  GBDW_CUDA(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
+  if (!g_own_stream) GBDW_CUDA(cudaStreamCreateWithFlags(&g_own_stream, cudaStreamNonBlocking));
+  if (!g_pinned) GBDW_CUDA(cudaMallocHost((void**)&g_pinned, 64 * sizeof(double)));
+  g_device_checked = 1;
+  return GBDW_OK;
+}
+
+int num_sms() { return g_num_sms > 0 ? g_num_sms : 152; }
+
+cudaStream_t stream() { return g_have_user_stream ? g_user_stream : g_own_stream; }
+
+void count_launch(uint64_t n) { g_launches += n; }
+
+void* scratch(size_t bytes, int slot) {
+  ScratchSlot& s = g_scratch[slot];
+  if (s.bytes >= bytes && s.p) return s.p;
+  if (s.p) {
+    cudaStreamSynchronize(stream());
+    cudaFree(s.p);
+    s.p = nullptr;
+    s.bytes = 0;
+  }
+  size_t want = bytes < (1u << 20) ? (1u << 20) : bytes;
+  if (cudaMalloc(&s.p, want) != cudaSuccess) {
+    cudaGetLastError();
+    s.p = nullptr;
+    return nullptr;
+  }
+  // zeroed in stream order: the library's stream does not synchronise with the legacy stream
+  if (cudaMemsetAsync(s.p, 0, want, stream()) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(s.p);
+    s.p = nullptr;
+    return nullptr;
+  }
+  s.bytes = want;
+  return s.p;
+}
+
+int reduce_scratch(int64_t nblocks, int width, Reduce* r) {
+  void* part = scratch(size_t(nblocks) * size_t(width) * sizeof(double), 0);
+  // slot 1: [counter (unsigned, padded to 64 B)] [result doubles]
+  void* ctl = scratch(4096, 1);
+  if (!part || !ctl) {
+    set_error("reduction scratch allocation failed");
+    return GBDW_ERR_ALLOC;
+  }
+  r->partials = (double*)part;
+  r->counter = (unsigned*)ctl;
+  r->result = (double*)((char*)ctl + 64);
+  return GBDW_OK;
+}
+
+int reduce_fetch(const Reduce& r, int width, double* host) {
+  GBDW_CUDA(cudaMemcpyAsync(g_pinned, r.result, size_t(width) * sizeof(double), cudaMemcpyDeviceToHost, stream()));
+  GBDW_CUDA(cudaStreamSynchronize(stream()));
+  for (int w = 0; w < width; ++w) host[w] = g_pinned[w];
+  return GBDW_OK;
+}
+
+namespace {
+__global__ void k_flush(uint4* p, size_t n, unsigned salt) {
+  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+    p[i] = make_uint4(unsigned(i) ^ salt, salt, unsigned(i >> 32), 0u);
+}
+}  // namespace
+
+}  // namespace gbdw
+
+using namespace gbdw;
+
+struct gbdw_timer {
+  cudaEvent_t a, b;
+};
+
+extern "C" {
+
+const char* gbdw_last_error(void) { return g_error.c_str(); }
+int gbdw_version(void) { return 100; }
+
+int gbdw_device_available(void) { return ensure_device() == GBDW_OK ? 1 : 0; }
+
+int gbdw_synchronize(void) {
+  if (int st = ensure_device()) return st;
+  GBDW_CUDA(cudaStreamSynchronize(stream()));
+  return GBDW_OK;
+}
+
+uint64_t gbdw_launch_count(void) { return g_launches.load(); }
+
+int gbdw_set_stream(void* s) {
+  g_user_stream = (cudaStream_t)s;
+  g_have_user_stream = (s != nullptr);
+  return GBDW_OK;
+}
+
+int gbdw_timer_create(gbdw_timer** t) {
+  if (!t) return GBDW_ERR_INVALID;
+  if (int st = ensure_device()) return st;
+  gbdw_timer* x = new gbdw_timer;
+  if (cudaEventCreate(&x->a) != cudaSuccess || cudaEventCreate(&x->b) != cudaSuccess) {
+    delete x;
+    return cuda_fail(cudaGetLastError(), "cudaEventCreate");
+  }
+  *t = x;
+  return GBDW_OK;
+}
+int gbdw_timer_start(gbdw_timer* t) {
+  if (!t) return GBDW_ERR_INVALID;
+  GBDW_CUDA(cudaEventRecord(t->a, stream()));
+  return GBDW_OK;
+}
+int gbdw_timer_stop(gbdw_timer* t, double* ms) {
+  if (!t) return GBDW_ERR_INVALID;
+  GBDW_CUDA(cudaEventRecord(t->b, stream()));
+  GBDW_CUDA(cudaEventSynchronize(t->b));
+  float f = 0.f;
+  GBDW_CUDA(cudaEventElapsedTime(&f, t->a, t->b));
+  if (ms) *ms = double(f);
+  return GBDW_OK;
+}
+int gbdw_timer_destroy(gbdw_timer* t) {
+  if (!t) return GBDW_OK;
+  cudaEventDestroy(t->a);
+  cudaEventDestroy(t->b);
+  delete t;
+  return GBDW_OK;
+}
+
+int gbdw_flush_l2(size_t nbytes) {
+  if (nbytes == 0) return GBDW_OK;
+  if (int st = ensure_device()) return st;
+  void* p = scratch(nbytes, 7);
+  if (!p) {
+    set_error("flush buffer allocation failed");
+    return GBDW_ERR_ALLOC;
+  }
+  static unsigned salt = 1;
+  k_flush<<<num_sms() * 4, 512, 0, stream()>>>((uint4*)p, nbytes / 16, salt++);
+  GBDW_LAUNCHED();
+  return GBDW_OK;
+}
+
+int gbdw_host_alloc(size_t nbytes, void** ptr) {
+  if (!ptr || nbytes == 0) return GBDW_ERR_INVALID;
+  if (int st = ensure_device()) return st;
+  GBDW_CUDA(cudaMallocHost(ptr, nbytes));
+  return GBDW_OK;
+}
+
+int gbdw_host_free(void* ptr) {
+  if (!ptr) return GBDW_OK;
+  GBDW_CUDA(cudaFreeHost(ptr));
+  return GBDW_OK;
+}
+
+}  // extern "C"

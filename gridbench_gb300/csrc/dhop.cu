@@ -1,0 +1,132 @@
+// Operator entry points: Dhop / DhopDag, the Shamir operator M / M^dagger and M^dagger M.
+#include "common.cuh"
+#include "dhop_kernel.cuh"
+#include "tune.h"
+
+namespace gbdw {
+
+namespace {
+
+bool combo_ok(const gbdw_gauge* g, const gbdw_field* f) {
+  if (f->prec == GBDW_F64) return g->prec == GBDW_F64;
+  if (f->prec == GBDW_F32) return g->prec == GBDW_F32;
+  return g->prec == GBDW_F16 || g->prec == GBDW_BF16;
+}
+
+}  // namespace
+
+int check_operands(const gbdw_gauge* g, const gbdw_field* out, const gbdw_field* in, bool need_single_rhs) {
+  if (!g || !out || !in) {
+    set_error("null gauge or field");
+    return GBDW_ERR_INVALID;
+  }
+  if (out == in) {
+    set_error("hopping kernels cannot run in place (out == in)");
+    return GBDW_ERR_INVALID;
+  }
+  if (in->lat != g->lat || out->lat != g->lat || in->nrhs != out->nrhs || in->prec != out->prec) {
+    set_error("gauge and fields must share lattice, nrhs and precision");
+    return GBDW_ERR_INVALID;
+  }
+  if (!combo_ok(g, in)) {
+    set_error("unsupported spinor/gauge precision pair (F64/F64, F32/F32, F16/F16, F16/BF16)");
+    return GBDW_ERR_INVALID;
+  }
+  if (need_single_rhs && in->nrhs != 1) {
+    set_error("the domain-wall operator takes single-right-hand-side fields");
+    return GBDW_ERR_INVALID;
+  }
+  return GBDW_OK;
+}
+
+DhopParams make_params(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in) {
+  DhopParams p;
+  p.U = g->d;
+  p.in = in->d;
+  p.in_norm = in->norm;
+  p.out = out->d;
+  p.out_norm = out->norm;
+  p.nbr4 = g->lat->nbr4;
+  p.nbr5 = g->lat->nbr5;
+  p.nsite = g->lat->nsite;
+  p.LsE = in->LsE;
+  p.Ls = g->lat->Ls;
+  p.a5 = 0.0;
+  p.mf = 0.0;
+  p.partials = nullptr;
+  p.counter = nullptr;
+  p.result = nullptr;
+  return p;
+}
+
+int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag, int epi, double a5, double mf,
+             double* norm2, bool fetch) {
+  if (int st = ensure_device()) return st;
+  DhopParams p = make_params(g, out, in);
+  p.a5 = a5;
+  p.mf = mf;
+  if (!g->lat->fast) {
+    if (epi || norm2 || in->nrhs != 1) {
+      set_error("general (non-factorisable) tables support the plain hopping term only");
+      return GBDW_ERR_INVALID;
+    }
+    return launch_dhop_general(p, in->prec, dag);
+  }
+  DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, epi);
+  if (in->LsE % L.spt != 0) L.spt = 1;
+  const int64_t nthreads = p.nsite * (p.LsE / L.spt);
+  const int64_t blocks = (nthreads + L.threads - 1) / L.threads;
+  Reduce red;
+  if (norm2) {
+    if (int st = reduce_scratch(blocks, 1, &red)) return st;
+    p.partials = red.partials;
+    p.counter = red.counter;
+    p.result = red.result;
+  }
+  int st;
+  if (in->prec == GBDW_F64) st = launch_dhop_f64(p, dag, epi, L);
+  else if (in->prec == GBDW_F32) st = launch_dhop_f32(p, dag, epi, L);
+  else st = launch_dhop_f16(p, g->prec, dag, epi, L);
+  if (st) return st;
+  if (norm2 && fetch) return reduce_fetch(red, 1, norm2);
+  return GBDW_OK;
+}
+
+}  // namespace gbdw
+
+using namespace gbdw;
+
+extern "C" {
+
+int gbdw_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag) {
+  if (int st = check_operands(g, out, in, false)) return st;
+  return run_dhop(g, out, in, dag ? 1 : 0, 0, 0.0, 0.0, nullptr);
+}
+
+int gbdw_dwf_m(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, double M5, double mf, int dag,
+               double* norm2) {
+  if (int st = check_operands(g, out, in, true)) return st;
+  return run_dhop(g, out, in, dag ? 1 : 0, 1, 5.0 - M5, mf, norm2);
+}
+
+int gbdw_dwf_mdagm(const gbdw_gauge* g, gbdw_field* out, gbdw_field* tmp, const gbdw_field* in, double M5, double mf,
+                   double* pap) {
+  if (int st = check_operands(g, tmp, in, true)) return st;
+  if (int st = check_operands(g, out, tmp, true)) return st;
+  if (out == in) {
+    set_error("gbdw_dwf_mdagm: out must differ from in");
+    return GBDW_ERR_INVALID;
+  }
+  // |M in|^2 is reduced by the first launch and read after the second, so the pair runs
+  // without a host round trip in between.
+  if (int st = run_dhop(g, tmp, in, 0, 1, 5.0 - M5, mf, pap, false)) return st;
+  if (int st = run_dhop(g, out, tmp, 1, 1, 5.0 - M5, mf, nullptr)) return st;
+  if (pap) {
+    Reduce red;
+    if (int st = reduce_scratch(1, 1, &red)) return st;
+    return reduce_fetch(red, 1, pap);
+  }
+  return GBDW_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,171 @@
+// Autotuner for the hopping kernel: times every admissible (threads per CTA, slices per
+// thread) pair on the caller's own fields with CUDA events and keeps the fastest, keyed by
+// (gauge precision, spinor precision, innermost extent Ls*nrhs, epilogue).  The cache can be
+// written to and read back from a small JSON object {"key": [threads, slices], ...}.
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+
+#include "common.cuh"
+#include "tune.h"
+
+namespace gbdw {
+
+namespace {
+std::map<std::string, DhopLaunch> g_tuned;
+std::mutex g_tune_mu;
+
+std::string key_of(int gprec, int sprec, int LsE, int epi) {
+  char buf[96];
+  snprintf(buf, sizeof buf, "g%d_s%d_L%d_e%d", gprec, sprec, LsE, epi);
+  return buf;
+}
+}  // namespace
+
+DhopLaunch default_launch(int gprec, int sprec, int LsE, int epi) {
+  (void)gprec;
+  (void)epi;
+  DhopLaunch L{128, 1};
+  if (sprec == GBDW_F32) L.spt = (LsE % 2 == 0) ? 2 : 1;
+  else if (sprec == GBDW_F16) L.spt = (LsE % 4 == 0) ? 4 : (LsE % 2 == 0) ? 2 : 1;
+  return L;
+}
+
+DhopLaunch tuned_launch(int gprec, int sprec, int LsE, int epi) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tuned.find(key_of(gprec, sprec, LsE, epi));
+  if (it != g_tuned.end()) return it->second;
+  return default_launch(gprec, sprec, LsE, epi);
+}
+
+void set_tuned_launch(int gprec, int sprec, int LsE, int epi, DhopLaunch L) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tuned[key_of(gprec, sprec, LsE, epi)] = L;
+}
+
+}  // namespace gbdw
+
+using namespace gbdw;
+
+extern "C" {
+
+int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag) {
+  if (int st = check_operands(g, out, in, false)) return st;
+  if (!g->lat->fast) return GBDW_OK;  // the general-table kernel has a single shape
+  if (int st = ensure_device()) return st;
+  const int threads_c[] = {64, 128, 256};
+  const int spt_c[] = {1, 2, 4};
+  cudaEvent_t a, b;
+  GBDW_CUDA(cudaEventCreate(&a));
+  GBDW_CUDA(cudaEventCreate(&b));
+  const DhopLaunch saved = tuned_launch(g->prec, in->prec, in->LsE, 0);
+  DhopLaunch best = saved;
+  float best_ms = 1e30f;
+  int status = GBDW_OK;
+  for (int spt : spt_c) {
+    if (in->LsE % spt != 0) continue;
+    if (in->prec == GBDW_F64 && spt > 2) continue;
+    for (int th : threads_c) {
+      DhopLaunch L{th, spt};
+      set_tuned_launch(g->prec, in->prec, in->LsE, 0, L);
+      for (int w = 0; w < 3 && !status; ++w) status = run_dhop(g, out, in, dag, 0, 0.0, 0.0, nullptr);
+      if (status) break;
+      const int reps = 10;
+      cudaEventRecord(a, stream());
+      for (int r = 0; r < reps && !status; ++r) status = run_dhop(g, out, in, dag, 0, 0.0, 0.0, nullptr);
+      cudaEventRecord(b, stream());
+      cudaEventSynchronize(b);
+      if (status) break;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, a, b);
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = L;
+      }
+    }
+    if (status) break;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  set_tuned_launch(g->prec, in->prec, in->LsE, 0, status ? saved : best);
+  // The M epilogue reads the centre site as well; reuse the choice for it.
+  if (!status && in->nrhs == 1) set_tuned_launch(g->prec, in->prec, in->LsE, 1, best);
+  return status;
+}
+
+int gbdw_tune_query(const gbdw_gauge* g, const gbdw_field* in, int cfg[2]) {
+  if (!g || !in || !cfg) return GBDW_ERR_INVALID;
+  const DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, 0);
+  cfg[0] = L.threads;
+  cfg[1] = L.spt;
+  return GBDW_OK;
+}
+
+int gbdw_tune_set(const gbdw_gauge* g, const gbdw_field* in, int threads, int spt) {
+  if (!g || !in || threads < 32 || threads > 256 || threads % 32 != 0 || !(spt == 1 || spt == 2 || spt == 4) ||
+      in->LsE % spt != 0 || (in->prec == GBDW_F64 && spt > 2)) {
+    set_error("gbdw_tune_set: threads must be 32..256 in steps of 32, spt 1/2/4 dividing Ls*nrhs (<= 2 for F64)");
+    return GBDW_ERR_INVALID;
+  }
+  set_tuned_launch(g->prec, in->prec, in->LsE, 0, DhopLaunch{threads, spt});
+  if (in->nrhs == 1) set_tuned_launch(g->prec, in->prec, in->LsE, 1, DhopLaunch{threads, spt});
+  return GBDW_OK;
+}
+
+int gbdw_tune_save(const char* path) {
+  if (!path) return GBDW_ERR_INVALID;
+  FILE* f = fopen(path, "w");
+  if (!f) {
+    set_error(std::string("cannot write tune cache ") + path);
+    return GBDW_ERR_INVALID;
+  }
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  fprintf(f, "{");
+  bool first = true;
+  for (auto& kv : g_tuned) {
+    fprintf(f, "%s\n  \"%s\": [%d, %d]", first ? "" : ",", kv.first.c_str(), kv.second.threads, kv.second.spt);
+    first = false;
+  }
+  fprintf(f, "\n}\n");
+  fclose(f);
+  return GBDW_OK;
+}
+
+int gbdw_tune_load(const char* path) {
+  if (!path) return GBDW_ERR_INVALID;
+  FILE* f = fopen(path, "r");
+  if (!f) {
+    set_error(std::string("cannot read tune cache ") + path);
+    return GBDW_ERR_INVALID;
+  }
+  std::string text;
+  char buf[4096];
+  size_t n;
+  while ((n = fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, n);
+  fclose(f);
+  // Entries look like "g1_s1_L16_e0": [128, 2]
+  size_t pos = 0;
+  int loaded = 0;
+  while ((pos = text.find('"', pos)) != std::string::npos) {
+    const size_t end = text.find('"', pos + 1);
+    if (end == std::string::npos) break;
+    const std::string key = text.substr(pos + 1, end - pos - 1);
+    int gp, sp, LsE, epi, th, spt;
+    const size_t lb = text.find('[', end);
+    if (lb == std::string::npos) break;
+    if (sscanf(key.c_str(), "g%d_s%d_L%d_e%d", &gp, &sp, &LsE, &epi) == 4 &&
+        sscanf(text.c_str() + lb, "[%d , %d]", &th, &spt) == 2 && th > 0 && th <= 256 && th % 32 == 0 &&
+        (spt == 1 || spt == 2 || spt == 4)) {
+      set_tuned_launch(gp, sp, LsE, epi, DhopLaunch{th, spt});
+      ++loaded;
+    }
+    pos = text.find(']', lb);
+    if (pos == std::string::npos) break;
+  }
+  (void)loaded;
+  return GBDW_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,14 @@
+// Launch-shape selection for the hopping kernel (threads per CTA, slices per thread).
+#pragma once
+#include "dhop_kernel.cuh"
+
+namespace gbdw {
+// Tuned entry if present, otherwise the built-in default for this precision and extent.
+DhopLaunch tuned_launch(int gprec, int sprec, int LsE, int epi);
+DhopLaunch default_launch(int gprec, int sprec, int LsE, int epi);
+void set_tuned_launch(int gprec, int sprec, int LsE, int epi, DhopLaunch L);
+int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag, int epi, double a5, double mf,
+             double* norm2, bool fetch = true);
+int check_operands(const gbdw_gauge* g, const gbdw_field* out, const gbdw_field* in, bool need_single_rhs);
+DhopParams make_params(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in);
+}  // namespace gbdw

@@ -1,0 +1,219 @@
+/*
+ * gbdw.h -- C ABI of the GB300 domain-wall Wilson hopping-term library (libgbdw.so).
+ *
+ * Plain C: opaque handles, plain pointers and sizes, integer status codes.  No CUDA or
+ * torch types appear in any signature, so the library can be bound from C, C++ (see
+ * gbdw_dslash.h), ctypes, cgo or JNI alike.
+ *
+ * Conventions shared with GridBench (reference file:line in brackets):
+ *   - spinor  Psi[(site*Ls + s)*12 + spin*3 + colour], complex, re/im interleaved
+ *     [dslash_simple.h:3,144]; with Nsimd SIMD lanes every complex becomes Nsimd complexes,
+ *     lane-minor [Simd_gpu_vec.h:110-128, bench.cc:105-139].
+ *   - doubled gauge field U[(site*8 + mu)*9 + row*3 + col], mu = Xp,Yp,Zp,Tp,Xm,Ym,Zm,Tm
+ *     [dslash_simple.h:5, WilsonKernelsHand.h:5-12]; U[mu+4](x) = U[mu](x - mu)^dagger.
+ *   - neighbour table nbr[(site*Ls + s)*8 + mu] = 5D spinor index, prm[...] = lane-permute
+ *     flag [TableGenerate.cc:75-91]; leg mu with prm set reads lane ^ (Nsimd >> (P+1)),
+ *     P = 3,2,1,0 for X,Y,Z,T [WilsonKernelsHandGpu.h:33-41].
+ *   - the output is the unscaled hopping sum, no -1/2 and no mass term [TableGenerate.cc:52].
+ *
+ * Every entry point returns GBDW_OK (0) or a positive gbdw_status; gbdw_last_error() gives
+ * the message.  Nothing in the library exits the process.
+ */
+#ifndef GBDW_H
+#define GBDW_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status / precision */
+
+typedef enum {
+  GBDW_OK = 0,
+  GBDW_ERR_INVALID = 1,       /* bad argument (null pointer, size, unsupported combination) */
+  GBDW_ERR_CUDA = 2,          /* a CUDA runtime call failed */
+  GBDW_ERR_ALLOC = 3,         /* device or pinned allocation failed */
+  GBDW_ERR_TABLE = 4,         /* neighbour table out of range */
+  GBDW_ERR_NOT_CONVERGED = 5, /* solver hit its iteration limit */
+  GBDW_ERR_DIVERGED = 6,      /* solver produced a non-finite or non-positive quantity */
+  GBDW_ERR_NO_DEVICE = 7      /* no CUDA device visible */
+} gbdw_status;
+
+/* Storage precision of a field.  Arithmetic is FP64 for GBDW_F64 and FP32 otherwise. */
+typedef enum {
+  GBDW_F64 = 0,  /* complex double */
+  GBDW_F32 = 1,  /* complex float */
+  GBDW_F16 = 2,  /* spinor: half2 per complex + one FP32 norm per 5D site;
+                    gauge : 12-real (two rows) half2, third row rebuilt as conj(r0 x r1) */
+  GBDW_BF16 = 3  /* gauge only: 12-real bf16 */
+} gbdw_prec;
+
+const char* gbdw_last_error(void);
+int gbdw_version(void);                 /* 100*major + minor */
+int gbdw_device_available(void);        /* 1 if a CUDA device can be used, else 0 */
+int gbdw_synchronize(void);             /* waits for the library stream */
+uint64_t gbdw_launch_count(void);       /* kernels this process launched through the library */
+int gbdw_set_stream(void* cuda_stream); /* NULL = the library's own non-blocking stream */
+
+/* ------------------------------------------------------------------ drop-in seam
+ * Replaces template<class Simd> double dslash_kernel(int nrep, Simd* Up, Simd* outp,
+ *   Simd* inp, uint64_t* nbr, uint64_t nsite, uint64_t Ls, uint8_t* prm)
+ *   [WilsonKernelsHand.h:17-18,25-26], called from bench.cc:148-164.
+ * prec is GBDW_F64 (vComplexD) or GBDW_F32 (vComplexF); nsimd is the lane count of the
+ * Simd type (1 for the dslash_simple layout).  nsite counts outer (SIMD) sites, as in the
+ * reference.  Pointers may be host (pageable or pinned) or device/managed memory: host
+ * buffers are copied in once per call and out once after the last repetition.  The
+ * hopping term is applied nrep times; *usec receives the device time of repetitions
+ * 1..nrep-1 (all of them when nrep == 1), mirroring WilsonKernelsHandCpu.h:407-450.
+ * dag = 1 applies DhopDag = gamma5 Dhop gamma5 (no counterpart in the reference). */
+int gbdw_dslash_kernel(int nrep, int prec, int nsimd, const void* U, void* out, const void* in,
+                       const uint64_t* nbr, uint64_t nsite, uint64_t Ls, const uint8_t* prm,
+                       int dag, double* usec);
+
+/* ------------------------------------------------------------------ generator
+ * Seeded equivalent of TableGenerate.cc:19-91 without Grid: random SU(3) links (Gaussian
+ * complex 3x3, Gram-Schmidt, det fixed to 1), the doubled field, i.i.d. N(0,1) source,
+ * and nbr/prm for a periodic lattice dims[4] = {Lx,Ly,Lz,Lt} laid out with nsimd lanes
+ * (1, 2, 4, 8 or 16; lanes split T first, then Z, Y, X, each split dimension halved).
+ * Outputs are in the reference layout, FP64.  Any output pointer may be NULL.
+ * Sizes (nsite = Lx*Ly*Lz*Lt / nsimd): U 144*nsite*nsimd doubles, phi 24*nsite*Ls*nsimd
+ * doubles, nbr and prm nsite*Ls*8 entries.  Deterministic across machines. */
+int gbdw_generate_gauge(const int dims[4], int nsimd, uint64_t seed, double* U);
+int gbdw_generate_fermion(const int dims[4], int Ls, int nsimd, uint64_t seed, double* phi);
+int gbdw_generate_table(const int dims[4], int Ls, int nsimd, uint64_t* nbr, uint8_t* prm);
+uint64_t gbdw_seed_from_ints(const int* seeds, int n);  /* e.g. {1,2,3,4} as in TableGenerate */
+
+/* ------------------------------------------------------------------ lattices and fields */
+
+/* Device-side random inputs for large workloads (same recipe as the generator above, but
+ * with CUDA's log/sincos, so the bits differ from gbdw_generate_*):
+ * gbdw_field_gaussian fills right-hand side rhs with i.i.d. N(0,1) re/im;
+ * gbdw_gauge_random creates a random SU(3) doubled gauge field (periodic lattices made by
+ * gbdw_lattice_create); equal seeds give the same field in every precision. */
+
+typedef struct gbdw_lattice gbdw_lattice;
+typedef struct gbdw_gauge gbdw_gauge;
+typedef struct gbdw_field gbdw_field;
+
+/* Lattice from a reference neighbour table (host or device pointers).  The table is
+ * range-checked; if every entry has the form nbr = nbr4(site,mu)*Ls + s with a permute
+ * flag independent of s, the 4D fast path is used, otherwise the general 5D gather. */
+int gbdw_lattice_from_table(gbdw_lattice** lat, uint64_t nsite, int Ls, int nsimd,
+                            const uint64_t* nbr, const uint8_t* prm);
+/* Periodic lattice built on the device (no table upload). */
+int gbdw_lattice_create(gbdw_lattice** lat, const int dims[4], int Ls);
+int gbdw_lattice_destroy(gbdw_lattice* lat);
+/* info[0]=sites (4D, lanes unrolled) info[1]=Ls info[2]=nsimd info[3]=fast path (1/0) */
+int gbdw_lattice_info(const gbdw_lattice* lat, int64_t info[4]);
+
+/* Gauge field stored at prec (F64, F32, F16 or BF16) from a reference-layout doubled
+ * field src (src_prec F64 or F32, host or device pointer). */
+int gbdw_gauge_create(gbdw_gauge** g, const gbdw_lattice* lat, int prec, const void* src,
+                      int src_prec);
+int gbdw_gauge_destroy(gbdw_gauge* g);
+
+/* Spinor field with nrhs right-hand sides (stored rhs-innermost so one gauge load serves
+ * Ls*nrhs slices). */
+int gbdw_field_create(gbdw_field** f, const gbdw_lattice* lat, int prec, int nrhs);
+int gbdw_field_destroy(gbdw_field* f);
+int gbdw_field_zero(gbdw_field* f);
+/* Copy one right-hand side in from / out to the reference layout (src/dst prec F64 or F32,
+ * host or device pointer). */
+int gbdw_field_import(gbdw_field* f, int rhs, const void* src, int src_prec);
+int gbdw_field_export(const gbdw_field* f, int rhs, void* dst, int dst_prec);
+/* dst = src with precision conversion (same lattice and nrhs). */
+int gbdw_field_copy(gbdw_field* dst, const gbdw_field* src);
+int gbdw_field_gaussian(gbdw_field* f, int rhs, uint64_t seed);
+int gbdw_gauge_random(gbdw_gauge** g, const gbdw_lattice* lat, int prec, uint64_t seed);
+
+/* ------------------------------------------------------------------ operators
+ * out = Dhop(in) (dag=0) or DhopDag(in) (dag=1) over all right-hand sides. */
+int gbdw_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag);
+
+/* Shamir domain-wall operator (no counterpart in the reference):
+ *   (M psi)(s) = (5 - M5) psi(s) - 1/2 Dhop psi(s) - P- psi(s+1) - P+ psi(s-1),
+ * P+- = (1 +- gamma5)/2, gamma5 = diag(1,1,-1,-1), and the s-wrap terms carry -mf.
+ * dag = 1 applies M^dagger.  If norm2 is non-NULL it receives |out|^2 (FP64 sum). */
+int gbdw_dwf_m(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, double M5, double mf,
+               int dag, double* norm2);
+/* out = M^dagger M in, tmp holds M in.  If pap is non-NULL it receives <in, out> = |M in|^2. */
+int gbdw_dwf_mdagm(const gbdw_gauge* g, gbdw_field* out, gbdw_field* tmp, const gbdw_field* in,
+                   double M5, double mf, double* pap);
+
+/* ------------------------------------------------------------------ BLAS-1 (FP64 sums) */
+int gbdw_norm2(const gbdw_field* x, double* out);
+int gbdw_dot(const gbdw_field* x, const gbdw_field* y, double* re, double* im); /* <x,y> */
+int gbdw_axpby(double a, const gbdw_field* x, double b, gbdw_field* y);          /* y=ax+by */
+
+/* ------------------------------------------------------------------ solvers
+ * Solve M^dagger M x = b for the Shamir operator.  mode:
+ *   GBDW_CG_PLAIN : FP32 operator, FP64 x/r/p vectors and sums, reliable updates with the
+ *                   FP64 operator (the plain FP32-kernel / FP64-residual solve);
+ *   GBDW_CG_MIXED : sloppy operator at sloppy_prec (F16 spinor + 12-real F16 gauge, or F32),
+ *                   low-precision inner vectors, reliable updates that recompute the true
+ *                   residual r = b - A x, the sums and the solution in FP64;
+ *   GBDW_CG_DOUBLE: everything FP64 (accuracy reference).
+ * b and x are FP64 fields.  Stops when the true relative residual |b-Ax|/|b| <= tol. */
+enum { GBDW_CG_PLAIN = 0, GBDW_CG_MIXED = 1, GBDW_CG_DOUBLE = 2 };
+typedef struct {
+  double tol;           /* target true relative residual, e.g. 1e-10 */
+  int max_iter;         /* iteration limit (GBDW_ERR_NOT_CONVERGED beyond it) */
+  double delta;         /* reliable-update threshold on |r|/max|r| (e.g. 0.1) */
+  int sloppy_prec;      /* GBDW_F16 or GBDW_F32 for GBDW_CG_MIXED */
+  int sloppy_gauge;     /* GBDW_F16, GBDW_BF16 or GBDW_F32 */
+} gbdw_cg_params;
+typedef struct {
+  int iterations;
+  int reliable_updates;
+  double true_residual;  /* |b - A x| / |b| in FP64 at exit */
+  double seconds;        /* wall time of the solve (device-synchronised) */
+  double final_rr;       /* last iterated |r|^2 / |b|^2 */
+} gbdw_cg_stats;
+int gbdw_cg_solve(const gbdw_gauge* g_double, const gbdw_gauge* g_single,
+                  const gbdw_gauge* g_sloppy, gbdw_field* x, const gbdw_field* b, double M5,
+                  double mf, int mode, const gbdw_cg_params* prm, gbdw_cg_stats* stats);
+
+/* ------------------------------------------------------------------ batched persistent Dhop
+ * Many independent instances (own lattice, gauge field, Ls and precision) in one persistent
+ * launch, replayed through a CUDA graph. */
+typedef struct gbdw_batch gbdw_batch;
+int gbdw_batch_create(gbdw_batch** b, int n, const gbdw_gauge* const* gauges,
+                      gbdw_field* const* outs, const gbdw_field* const* ins, int dag);
+int gbdw_batch_run(gbdw_batch* b);        /* one graph replay */
+int gbdw_batch_destroy(gbdw_batch* b);
+/* info[0]=work items info[1]=persistent CTAs info[2]=threads per CTA info[3]=graph (1/0) */
+int gbdw_batch_info(const gbdw_batch* b, int64_t info[4]);
+
+/* ------------------------------------------------------------------ autotuner
+ * Times the launch shapes of the hopping kernel for (g, field) and stores the fastest in
+ * the process cache and, if path is non-NULL, in a JSON file read back by gbdw_tune_load.
+ * Untuned shapes use built-in defaults. */
+int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag);
+int gbdw_tune_load(const char* path);
+int gbdw_tune_save(const char* path);
+/* Writes the chosen (threads per CTA, slices per thread) for a field into cfg[2]. */
+int gbdw_tune_query(const gbdw_gauge* g, const gbdw_field* in, int cfg[2]);
+/* Pins the shape for fields like `in` (threads a multiple of 32 up to 256; slices per thread
+ * 1, 2 or 4 dividing Ls*nrhs, at most 2 for F64). */
+int gbdw_tune_set(const gbdw_gauge* g, const gbdw_field* in, int threads, int spt);
+
+/* ------------------------------------------------------------------ timing on the library stream */
+typedef struct gbdw_timer gbdw_timer;
+int gbdw_timer_create(gbdw_timer** t);
+int gbdw_timer_start(gbdw_timer* t);
+int gbdw_timer_stop(gbdw_timer* t, double* ms); /* synchronises, returns elapsed ms */
+int gbdw_timer_destroy(gbdw_timer* t);
+/* Writes nbytes of junk through a scratch buffer to evict L2 (no-op if nbytes == 0). */
+int gbdw_flush_l2(size_t nbytes);
+
+/* Page-locked host memory for fast host<->device copies of reference-layout buffers. */
+int gbdw_host_alloc(size_t nbytes, void** ptr);
+int gbdw_host_free(void* ptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBDW_H */

@@ -1,0 +1,206 @@
+"""GPU hopping term (FP64/FP32, Dhop/DhopDag) against the oracle, the reference's golden
+vectors, the drop-in seam, lane layouts, general tables and full-size properties."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import gridbench_gb300 as gb
+import oracle
+from conftest import GOLDEN, make_case, rel_err
+
+pytestmark = pytest.mark.gpu
+
+TOL = {gb.F64: 1e-12, gb.F32: 1e-6}  # relative to the FP64 oracle (spec bar for FP32)
+
+
+def _run(c, prec, dag=0, nrhs=1):
+    lat = gb.Lattice.from_table(c["nbr"], c["prm"], c["nsite"], c["Ls"], c["nsimd"])
+    g = gb.Gauge(lat, c["U"], prec)
+    x = gb.Field(lat, prec).load(c["phi"])
+    y = gb.Field(lat, prec)
+    gb.dhop(g, y, x, dag)
+    return y.numpy(), lat
+
+
+@pytest.mark.parametrize("dims,Ls", [((2, 2, 2, 2), 4), ((4, 4, 4, 4), 4), ((4, 2, 6, 2), 3), ((8, 8, 8, 8), 8)])
+@pytest.mark.parametrize("prec", [gb.F64, gb.F32])
+@pytest.mark.parametrize("dag", [0, 1])
+def test_dhop_matches_oracle(gpu, dims, Ls, prec, dag):
+    c = make_case(dims, Ls)
+    ref = oracle.dslash(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], Ls, dag)
+    out, lat = _run(c, prec, dag)
+    assert lat.info()["fast"]
+    assert rel_err(out, ref) < TOL[prec]
+
+
+@pytest.mark.parametrize("f", sorted(glob.glob(os.path.join(GOLDEN, "golden_simple_*.npz"))))
+def test_fp64_matches_dslash_simple_golden(gpu, f):
+    g = np.load(f)
+    c = make_case(tuple(g["dims"]), int(g["Ls"]))
+    out, _ = _run(c, gb.F64)
+    assert rel_err(out, g["psi"]) < 1e-13
+    # the reference's own check: sum of squared differences <= 1e-10 (bench_simple.cc:114-119)
+    assert float(np.sum((out - g["psi"]) ** 2)) <= 1e-10
+
+
+@pytest.mark.parametrize("f", sorted(glob.glob(os.path.join(GOLDEN, "golden_hand_*.npz"))))
+def test_dropin_lane_layout_matches_hand_kernel_golden(gpu, f):
+    """bench.cc's VGPU flow: Nsimd-lane data through dslash_kernel, compared with the
+    reference's AVX-512 hand kernel output on the same data."""
+    g = np.load(f)
+    ns = int(g["nsimd"])
+    dt = np.float64 if "f64" in os.path.basename(f) else np.float32
+    c = make_case(tuple(g["dims"]), int(g["Ls"]), ns)
+    U = c["U"].astype(dt)
+    phi = c["phi"].astype(dt)
+    out = np.zeros_like(phi)
+    usec = gb.dslash_kernel(3, U, out, phi, c["nbr"], c["nsite"], c["Ls"], c["prm"], nsimd=ns)
+    assert usec > 0
+    assert rel_err(out, g["psi"]) < (1e-13 if dt == np.float64 else 1e-6)
+
+
+@pytest.mark.parametrize("nsimd", [2, 4, 8, 16])
+@pytest.mark.parametrize("dag", [0, 1])
+def test_lane_layouts_match_oracle(gpu, nsimd, dag):
+    c = make_case((4, 4, 4, 4), 4, nsimd)
+    ref = oracle.dslash_lanes(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], 4, nsimd, dag)
+    out = np.zeros_like(c["phi"])
+    # the seam has no dag argument in the reference; use the object API for dag
+    lat = gb.Lattice.from_table(c["nbr"], c["prm"], c["nsite"], 4, nsimd)
+    g = gb.Gauge(lat, c["U"], gb.F64)
+    x = gb.Field(lat, gb.F64).load(c["phi"])
+    y = gb.Field(lat, gb.F64)
+    gb.dhop(g, y, x, dag)
+    assert rel_err(y.numpy(), ref) < 1e-13
+    if dag == 0:
+        gb.dslash_kernel(1, c["U"].copy(), out, c["phi"], c["nbr"], c["nsite"], 4, c["prm"], nsimd=nsimd)
+        assert rel_err(out, ref) < 1e-13
+
+
+def test_dslash_kernel_dropin_nrep_and_timing(gpu):
+    c = make_case((4, 4, 4, 4), 8)
+    ref = oracle.dslash(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], 8)
+    for dt, tol in ((np.float64, 1e-13), (np.float32, 1e-6)):
+        out = np.zeros(c["phi"].shape, dtype=dt)
+        usec = gb.dslash_kernel(5, c["U"].astype(dt), out, c["phi"].astype(dt), c["nbr"], c["nsite"], 8, c["prm"])
+        assert usec > 0
+        assert rel_err(out, ref) < tol
+
+
+def test_general_table_path(gpu):
+    """A table that does not factorise into nbr4*Ls + s runs on the general gather kernel
+    and still follows the table exactly (the reference kernel obeys any table)."""
+    c = make_case((4, 4, 2, 2), 4)
+    t = c["nbr"].reshape(c["nsite"], 4, 8).copy()
+    Ls = 4
+    # X-forward leg also steps one slice in s
+    site = t[:, :, 0] // Ls
+    s = t[:, :, 0] % Ls
+    t[:, :, 0] = site * Ls + (s + 1) % Ls
+    nbr = t.ravel()
+    ref = oracle.dslash(c["U"], c["phi"], nbr, c["prm"], c["nsite"], Ls)
+    for prec in (gb.F64, gb.F32):
+        lat = gb.Lattice.from_table(nbr, c["prm"], c["nsite"], Ls)
+        assert not lat.info()["fast"]
+        g = gb.Gauge(lat, c["U"], prec)
+        x = gb.Field(lat, prec).load(c["phi"])
+        y = gb.Field(lat, prec)
+        gb.dhop(g, y, x)
+        assert rel_err(y.numpy(), ref) < TOL[prec]
+
+
+def test_table_out_of_range_is_rejected(gpu):
+    c = make_case((2, 2, 2, 2), 2)
+    nbr = c["nbr"].copy()
+    nbr[5] = c["nsite"] * 2 + 7
+    with pytest.raises(gb.GbdwError) as e:
+        gb.Lattice.from_table(nbr, c["prm"], c["nsite"], 2)
+    assert e.value.status == 4
+
+
+@pytest.mark.parametrize("prec,spts", [(gb.F32, (1, 2, 4)), (gb.F64, (1, 2))])
+@pytest.mark.parametrize("threads", [64, 128, 256])
+def test_every_launch_shape(gpu, prec, spts, threads):
+    c = make_case((4, 4, 4, 4), 8)
+    ref = oracle.dslash(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], 8)
+    lat = gb.Lattice.from_table(c["nbr"], c["prm"], c["nsite"], 8)
+    g = gb.Gauge(lat, c["U"], prec)
+    x = gb.Field(lat, prec).load(c["phi"])
+    y = gb.Field(lat, prec)
+    for spt in spts:
+        gb.tune_set(g, x, threads, spt)
+        gb.dhop(g, y, x)
+        assert rel_err(y.numpy(), ref) < TOL[prec], (threads, spt)
+    gb.tune_set(g, x, 128, spts[-1] if prec == gb.F64 else 2)
+
+
+def test_periodic_lattice_equals_table_lattice(gpu):
+    c = make_case((4, 6, 2, 4), 4)
+    ref = oracle.dslash(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], 4)
+    lat = gb.Lattice.periodic((4, 6, 2, 4), 4)
+    g = gb.Gauge(lat, c["U"], gb.F64)
+    x = gb.Field(lat, gb.F64).load(c["phi"])
+    y = gb.Field(lat, gb.F64)
+    gb.dhop(g, y, x)
+    assert rel_err(y.numpy(), ref) < 1e-13
+
+
+def test_multi_rhs_equals_single_rhs(gpu):
+    dims, Ls, k = (4, 4, 4, 4), 4, 3
+    c = make_case(dims, Ls)
+    lat = gb.Lattice.from_table(c["nbr"], c["prm"], c["nsite"], Ls)
+    g = gb.Gauge(lat, c["U"], gb.F32)
+    X = gb.Field(lat, gb.F32, k)
+    Y = gb.Field(lat, gb.F32, k)
+    srcs = [gb.generate_fermion(dims, Ls, 1, (5 + r, 6, 7, 8)) for r in range(k)]
+    for r in range(k):
+        X.load(srcs[r], r)
+    gb.dhop(g, Y, X)
+    for r in range(k):
+        ref = oracle.dslash(c["U"], srcs[r], c["nbr"], c["prm"], c["nsite"], Ls)
+        assert rel_err(Y.numpy(r), ref) < 1e-6
+
+
+def test_full_size_properties_16x16(gpu):
+    """16^4 x 16 (the roofline workload): FP32 within 1e-6 of the GPU FP64 result, DhopDag
+    adjoint to Dhop, linearity -- properties that do not need the CPU oracle at full size."""
+    dims, Ls = (16, 16, 16, 16), 16
+    lat = gb.Lattice.periodic(dims, Ls)
+    U = gb.generate_gauge(dims)
+    g64 = gb.Gauge(lat, U, gb.F64)
+    g32 = gb.Gauge(lat, U, gb.F32)
+    a = gb.generate_fermion(dims, Ls)
+    b = gb.generate_fermion(dims, Ls, 1, (9, 10, 11, 12))
+    x64 = gb.Field(lat, gb.F64).load(a)
+    y64 = gb.Field(lat, gb.F64)
+    x32 = gb.Field(lat, gb.F32).load(a)
+    y32 = gb.Field(lat, gb.F32)
+    for dag in (0, 1):
+        gb.dhop(g64, y64, x64, dag)
+        gb.dhop(g32, y32, x32, dag)
+        d = gb.Field(lat, gb.F64)
+        d.copy_from(y32)
+        d.axpby(-1.0, y64, 1.0)
+        assert np.sqrt(d.norm2() / y64.norm2()) < 1e-6
+    # <b, D a> == <Ddag b, a>
+    bf = gb.Field(lat, gb.F64).load(b)
+    Da = gb.Field(lat, gb.F64)
+    Ddb = gb.Field(lat, gb.F64)
+    gb.dhop(g64, Da, x64, 0)
+    gb.dhop(g64, Ddb, bf, 1)
+    lhs = bf.dot(Da)
+    rhs = Ddb.dot(x64)
+    assert abs(lhs - rhs) / abs(lhs) < 1e-12
+    # linearity: D(2a + b) = 2 Da + Db
+    s = gb.Field(lat, gb.F64)
+    s.copy_from(bf)
+    s.axpby(2.0, x64, 1.0)
+    Ds = gb.Field(lat, gb.F64)
+    gb.dhop(g64, Ds, s, 0)
+    Db = gb.Field(lat, gb.F64)
+    gb.dhop(g64, Db, bf, 0)
+    Ds.axpby(-2.0, Da, 1.0)
+    Ds.axpby(-1.0, Db, 1.0)
+    assert np.sqrt(Ds.norm2() / Db.norm2()) < 1e-13
