@@ -433,7 +433,8 @@ def run_ours(args, D: Dist) -> dict | None:
         "config": {"workload": "FP32 domain-wall Wilson Dhop, 16^4 x Ls=16, periodic", "lattice": list(DIMS),
                    "Ls": LS, "parallelism": "replicas" if D.world > 1 else "single",
                    "l2": "inputs larger than L2: two alternating in/out pairs, 476 MB vs 129 MB L2",
-                   "launch": {"threads": cfg[0], "slices_per_thread": cfg[1]}},
+                   "launch": {"threads": cfg[0], "slices_per_thread": cfg[1],
+                              "form": "tma-staged" if cfg[2] == 1 else "direct", "stages": cfg[3]}},
         "rel_err_vs_fp64": rel,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,

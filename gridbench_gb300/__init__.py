@@ -255,13 +255,14 @@ def tune_dhop(g: Gauge, out: Field, inp: Field, dag: int = 0) -> tuple:
 
 
 def tune_query(g: Gauge, inp: Field) -> tuple:
-    cfg = (C.c_int * 2)()
+    """(threads per CTA, slices per thread, form 0 direct / 1 TMA-staged, stages)"""
+    cfg = (C.c_int * 4)()
     check(load().gbdw_tune_query(g.h, inp.h, cfg))
-    return int(cfg[0]), int(cfg[1])
+    return tuple(int(v) for v in cfg)
 
 
-def tune_set(g: Gauge, inp: Field, threads: int, spt: int):
-    check(load().gbdw_tune_set(g.h, inp.h, threads, spt))
+def tune_set(g: Gauge, inp: Field, threads: int, spt: int, form: int = 0, stages: int = 4):
+    check(load().gbdw_tune_set(g.h, inp.h, threads, spt, form, stages))
 
 
 def tune_save(path: str):

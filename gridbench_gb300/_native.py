@@ -15,8 +15,9 @@ OK, ERR_INVALID, ERR_CUDA, ERR_ALLOC, ERR_TABLE, ERR_NOT_CONVERGED, ERR_DIVERGED
 F64, F32, F16, BF16 = 0, 1, 2, 3
 CG_PLAIN, CG_MIXED, CG_DOUBLE = 0, 1, 2
 
+ERR_TIMEOUT = 8
 STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "ALLOC", 4: "TABLE", 5: "NOT_CONVERGED",
-                6: "DIVERGED", 7: "NO_DEVICE"}
+                6: "DIVERGED", 7: "NO_DEVICE", 8: "TIMEOUT"}
 
 
 class GbdwError(RuntimeError):
@@ -85,7 +86,8 @@ PROTOTYPES = {
     "gbdw_tune_load": (_i, [C.c_char_p]),
     "gbdw_tune_save": (_i, [C.c_char_p]),
     "gbdw_tune_query": (_i, [_vp, _vp, C.POINTER(C.c_int)]),
-    "gbdw_tune_set": (_i, [_vp, _vp, _i, _i]),
+    "gbdw_tune_set": (_i, [_vp, _vp, _i, _i, _i, _i]),
+    "gbdw_selftest_wait_timeout": (_i, [_u64]),
     "gbdw_timer_create": (_i, [_pp]),
     "gbdw_timer_start": (_i, [_vp]),
     "gbdw_timer_stop": (_i, [_vp, _dp]),

@@ -28,6 +28,7 @@ void count_launch(uint64_t n = 1);
 void* scratch(size_t bytes, int slot);
 int ensure_device();
 int num_sms();
+unsigned* device_error_word();  // set by kernels whose bounded waits expired
 
 #define GBDW_CUDA(call)                                       \
   do {                                                        \

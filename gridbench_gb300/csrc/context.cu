@@ -103,6 +103,11 @@ int reduce_scratch(int64_t nblocks, int width, Reduce* r) {
   return GBDW_OK;
 }
 
+unsigned* device_error_word() {
+  void* ctl = scratch(4096, 1);
+  return ctl ? (unsigned*)((char*)ctl + 2048) : nullptr;
+}
+
 int reduce_fetch(const Reduce& r, int width, double* host) {
   GBDW_CUDA(cudaMemcpyAsync(g_pinned, r.result, size_t(width) * sizeof(double), cudaMemcpyDeviceToHost, stream()));
   GBDW_CUDA(cudaStreamSynchronize(stream()));
@@ -135,6 +140,15 @@ int gbdw_device_available(void) { return ensure_device() == GBDW_OK ? 1 : 0; }
 int gbdw_synchronize(void) {
   if (int st = ensure_device()) return st;
   GBDW_CUDA(cudaStreamSynchronize(stream()));
+  unsigned* w = device_error_word();
+  if (!w) return GBDW_ERR_ALLOC;
+  unsigned h = 0;
+  GBDW_CUDA(cudaMemcpy(&h, w, sizeof h, cudaMemcpyDeviceToHost));
+  if (h) {
+    GBDW_CUDA(cudaMemset(w, 0, sizeof h));
+    set_error("a kernel's bounded wait expired (device error word " + std::to_string(h) + ")");
+    return GBDW_ERR_TIMEOUT;
+  }
   return GBDW_OK;
 }
 

@@ -56,6 +56,7 @@ DhopParams make_params(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* i
   p.partials = nullptr;
   p.counter = nullptr;
   p.result = nullptr;
+  p.err = device_error_word();
   return p;
 }
 
@@ -72,10 +73,17 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
     }
     return launch_dhop_general(p, in->prec, dag);
   }
+  if (!p.err) {
+    set_error("device error word allocation failed");
+    return GBDW_ERR_ALLOC;
+  }
   DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, epi);
   if (in->LsE % L.spt != 0) L.spt = 1;
+  int NS = 0, tthreads = 0;
+  size_t smem = 0;
+  if (L.mode == 1 && !tma_shape(in->prec, in->LsE, L, &NS, &tthreads, &smem)) L.mode = 0;
   const int64_t nthreads = p.nsite * (p.LsE / L.spt);
-  const int64_t blocks = (nthreads + L.threads - 1) / L.threads;
+  const int64_t blocks = L.mode == 1 ? (p.nsite + NS - 1) / NS : (nthreads + L.threads - 1) / L.threads;
   Reduce red;
   if (norm2) {
     if (int st = reduce_scratch(blocks, 1, &red)) return st;
@@ -90,6 +98,25 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
   if (st) return st;
   if (norm2 && fetch) return reduce_fetch(red, 1, norm2);
   return GBDW_OK;
+}
+
+bool tma_shape(int prec, int LsE, DhopLaunch L, int* NS, int* threads, size_t* smem) {
+  if (L.spt < 1 || LsE % L.spt != 0) return false;
+  if (prec == GBDW_F16 && LsE % 4 != 0) return false;  // the norm block must be a 16-byte multiple
+  const int Tps = LsE / L.spt;
+  if (Tps > 256) return false;
+  int ns = L.threads / Tps > 1 ? L.threads / Tps : 1;
+  auto round32 = [](int t) { return (t + 31) / 32 * 32; };  // whole warps (grid_sum shuffles)
+  while (ns > 1 && round32(ns * Tps) > 256) --ns;
+  if (round32(ns * Tps) > 256) return false;
+  const size_t esz = spinor_elem_bytes(prec);
+  const size_t stage = size_t(ns) * (12 * size_t(LsE) * esz + (prec == GBDW_F16 ? 4 * size_t(LsE) : 0));
+  const size_t sm = size_t(L.stages) * stage + size_t(L.stages) * 8;
+  if (sm > 227 * 1024) return false;
+  *NS = ns;
+  *threads = round32(ns * Tps);
+  *smem = sm;
+  return true;
 }
 
 }  // namespace gbdw

@@ -316,6 +316,7 @@ struct DhopParams {
   double* partials;      // fused |out|^2 when non-null
   unsigned* counter;
   double* result;
+  unsigned* err;         // device error word (bounded waits that expired)
 };
 
 // Writes N slices of result spinor v[N][12] at element eo (and norms at no for F16);
@@ -518,8 +519,10 @@ __global__ void __launch_bounds__(256) k_dhop_general(const DhopParams p) {
 
 // ------------------------------------------------------------------ launch dispatch
 struct DhopLaunch {
-  int threads;  // per CTA
-  int spt;      // slices per thread
+  int threads;     // per CTA (target; the staged kernel rounds to whole sites)
+  int spt;         // slices per thread
+  int mode = 0;    // 0: direct loads, 1: TMA-staged neighbour blocks
+  int stages = 4;  // staged kernel: depth of the leg ring
 };
 
 // Implemented per precision family in dhop_f64.cu / dhop_f32.cu / dhop_f16.cu.
@@ -527,5 +530,7 @@ int launch_dhop_f64(const DhopParams& p, int dag, int epi, DhopLaunch L);
 int launch_dhop_f32(const DhopParams& p, int dag, int epi, DhopLaunch L);
 int launch_dhop_f16(const DhopParams& p, int gprec, int dag, int epi, DhopLaunch L);
 int launch_dhop_general(const DhopParams& p, int prec, int dag);
+// Sites per CTA and dynamic shared memory of the staged kernel, or false if it cannot run.
+bool tma_shape(int prec, int LsE, DhopLaunch L, int* NS, int* threads, size_t* smem);
 
 }  // namespace gbdw

@@ -1,0 +1,59 @@
+// Launch dispatch shared by the per-precision units: maps a runtime (dag, epilogue, slices
+// per thread, form, stages) choice onto the compiled kernel instances.
+#pragma once
+#include "dhop_kernel.cuh"
+#include "dhop_tma.cuh"
+
+namespace gbdw {
+
+template <int PIN, int POUT, int GP, int DAG, int N, int EPI>
+int go_direct(const DhopParams& p, DhopLaunch L) {
+  const int64_t nthreads = p.nsite * (p.LsE / N);
+  const unsigned blocks = unsigned((nthreads + L.threads - 1) / L.threads);
+  k_dhop<PIN, POUT, GP, DAG, N, EPI><<<blocks, L.threads, 0, stream()>>>(p);
+  GBDW_LAUNCHED();
+  return GBDW_OK;
+}
+
+template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int STAGES>
+int go_tma(const DhopParams& p, DhopLaunch L) {
+  int NS = 0, threads = 0;
+  size_t smem = 0;
+  if (!tma_shape(PIN, p.LsE, L, &NS, &threads, &smem)) {
+    set_error("staged hopping kernel: no admissible shape for this extent");
+    return GBDW_ERR_INVALID;
+  }
+  auto kern = k_dhop_tma<PIN, POUT, GP, DAG, N, EPI, STAGES>;
+  static bool opted_in = false;  // one attribute call per instance
+  if (!opted_in) {
+    GBDW_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    opted_in = true;
+  }
+  const unsigned blocks = unsigned((p.nsite + NS - 1) / NS);
+  kern<<<blocks, threads, smem, stream()>>>(p, NS);
+  GBDW_LAUNCHED();
+  return GBDW_OK;
+}
+
+// Slice splits compiled per precision: S1 and S2 for both forms.
+template <int PIN, int POUT, int GP, int DAG, int EPI, int S1, int S2>
+int by_shape(const DhopParams& p, DhopLaunch L) {
+  if (L.mode == 1) {
+    if (L.spt == S1) return L.stages == 2 ? go_tma<PIN, POUT, GP, DAG, S1, EPI, 2>(p, L) : go_tma<PIN, POUT, GP, DAG, S1, EPI, 4>(p, L);
+    if (L.spt == S2) return L.stages == 2 ? go_tma<PIN, POUT, GP, DAG, S2, EPI, 2>(p, L) : go_tma<PIN, POUT, GP, DAG, S2, EPI, 4>(p, L);
+  } else {
+    if (L.spt == 1) return go_direct<PIN, POUT, GP, DAG, 1, EPI>(p, L);
+    if (L.spt == 2) return go_direct<PIN, POUT, GP, DAG, 2, EPI>(p, L);
+    if (L.spt == 4 && PIN != GBDW_F64) return go_direct<PIN, POUT, GP, DAG, (PIN == GBDW_F64 ? 2 : 4), EPI>(p, L);
+  }
+  set_error("hopping kernel: slices per thread not compiled for this precision and form");
+  return GBDW_ERR_INVALID;
+}
+
+template <int PIN, int POUT, int GP, int S1, int S2>
+int dispatch(const DhopParams& p, int dag, int epi, DhopLaunch L) {
+  if (dag) return epi ? by_shape<PIN, POUT, GP, 1, 1, S1, S2>(p, L) : by_shape<PIN, POUT, GP, 1, 0, S1, S2>(p, L);
+  return epi ? by_shape<PIN, POUT, GP, 0, 1, S1, S2>(p, L) : by_shape<PIN, POUT, GP, 0, 0, S1, S2>(p, L);
+}
+
+}  // namespace gbdw

@@ -7,6 +7,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "common.cuh"
 #include "tune.h"
@@ -55,8 +56,24 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
   if (int st = check_operands(g, out, in, false)) return st;
   if (!g->lat->fast) return GBDW_OK;  // the general-table kernel has a single shape
   if (int st = ensure_device()) return st;
+  // candidate shapes: direct loads with 1/2/4 slices per thread, and the TMA-staged form
+  // with the slice splits compiled for this precision and 2 or 4 stages
+  std::vector<DhopLaunch> cands;
   const int threads_c[] = {64, 128, 256};
-  const int spt_c[] = {1, 2, 4};
+  const int s1 = in->prec == GBDW_F16 ? 2 : 1, s2 = in->prec == GBDW_F16 ? 4 : 2;
+  for (int th : threads_c) {
+    for (int spt : {1, 2, 4}) {
+      if (in->LsE % spt != 0 || (in->prec == GBDW_F64 && spt > 2)) continue;
+      cands.push_back(DhopLaunch{th, spt, 0, 4});
+    }
+    for (int spt : {s1, s2})
+      for (int stages : {2, 4}) {
+        DhopLaunch L{th, spt, 1, stages};
+        int ns, tt;
+        size_t sm;
+        if (tma_shape(in->prec, in->LsE, L, &ns, &tt, &sm)) cands.push_back(L);
+      }
+  }
   cudaEvent_t a, b;
   GBDW_CUDA(cudaEventCreate(&a));
   GBDW_CUDA(cudaEventCreate(&b));
@@ -64,28 +81,22 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
   DhopLaunch best = saved;
   float best_ms = 1e30f;
   int status = GBDW_OK;
-  for (int spt : spt_c) {
-    if (in->LsE % spt != 0) continue;
-    if (in->prec == GBDW_F64 && spt > 2) continue;
-    for (int th : threads_c) {
-      DhopLaunch L{th, spt};
-      set_tuned_launch(g->prec, in->prec, in->LsE, 0, L);
-      for (int w = 0; w < 3 && !status; ++w) status = run_dhop(g, out, in, dag, 0, 0.0, 0.0, nullptr);
-      if (status) break;
-      const int reps = 10;
-      cudaEventRecord(a, stream());
-      for (int r = 0; r < reps && !status; ++r) status = run_dhop(g, out, in, dag, 0, 0.0, 0.0, nullptr);
-      cudaEventRecord(b, stream());
-      cudaEventSynchronize(b);
-      if (status) break;
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, a, b);
-      if (ms < best_ms) {
-        best_ms = ms;
-        best = L;
-      }
-    }
+  for (const DhopLaunch& L : cands) {
+    set_tuned_launch(g->prec, in->prec, in->LsE, 0, L);
+    for (int w = 0; w < 3 && !status; ++w) status = run_dhop(g, out, in, dag, 0, 0.0, 0.0, nullptr);
     if (status) break;
+    const int reps = 10;
+    cudaEventRecord(a, stream());
+    for (int r = 0; r < reps && !status; ++r) status = run_dhop(g, out, in, dag, 0, 0.0, 0.0, nullptr);
+    cudaEventRecord(b, stream());
+    cudaEventSynchronize(b);
+    if (status) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = L;
+    }
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
@@ -100,17 +111,31 @@ int gbdw_tune_query(const gbdw_gauge* g, const gbdw_field* in, int cfg[2]) {
   const DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, 0);
   cfg[0] = L.threads;
   cfg[1] = L.spt;
+  cfg[2] = L.mode;
+  cfg[3] = L.stages;
   return GBDW_OK;
 }
 
-int gbdw_tune_set(const gbdw_gauge* g, const gbdw_field* in, int threads, int spt) {
+int gbdw_tune_set(const gbdw_gauge* g, const gbdw_field* in, int threads, int spt, int form, int stages) {
   if (!g || !in || threads < 32 || threads > 256 || threads % 32 != 0 || !(spt == 1 || spt == 2 || spt == 4) ||
-      in->LsE % spt != 0 || (in->prec == GBDW_F64 && spt > 2)) {
-    set_error("gbdw_tune_set: threads must be 32..256 in steps of 32, spt 1/2/4 dividing Ls*nrhs (<= 2 for F64)");
+      in->LsE % spt != 0 || (in->prec == GBDW_F64 && spt > 2) || (form != 0 && form != 1) ||
+      (stages != 2 && stages != 4)) {
+    set_error("gbdw_tune_set: threads 32..256 in steps of 32, spt 1/2/4 dividing Ls*nrhs (<= 2 for F64), "
+              "form 0/1, stages 2/4");
     return GBDW_ERR_INVALID;
   }
-  set_tuned_launch(g->prec, in->prec, in->LsE, 0, DhopLaunch{threads, spt});
-  if (in->nrhs == 1) set_tuned_launch(g->prec, in->prec, in->LsE, 1, DhopLaunch{threads, spt});
+  const DhopLaunch L{threads, spt, form, stages};
+  if (form == 1) {
+    const int s1 = in->prec == GBDW_F16 ? 2 : 1, s2 = in->prec == GBDW_F16 ? 4 : 2;
+    int ns, tt;
+    size_t sm;
+    if ((spt != s1 && spt != s2) || !tma_shape(in->prec, in->LsE, L, &ns, &tt, &sm)) {
+      set_error("gbdw_tune_set: the staged form is not available for this shape");
+      return GBDW_ERR_INVALID;
+    }
+  }
+  set_tuned_launch(g->prec, in->prec, in->LsE, 0, L);
+  if (in->nrhs == 1) set_tuned_launch(g->prec, in->prec, in->LsE, 1, L);
   return GBDW_OK;
 }
 
@@ -125,7 +150,8 @@ int gbdw_tune_save(const char* path) {
   fprintf(f, "{");
   bool first = true;
   for (auto& kv : g_tuned) {
-    fprintf(f, "%s\n  \"%s\": [%d, %d]", first ? "" : ",", kv.first.c_str(), kv.second.threads, kv.second.spt);
+    fprintf(f, "%s\n  \"%s\": [%d, %d, %d, %d]", first ? "" : ",", kv.first.c_str(), kv.second.threads,
+            kv.second.spt, kv.second.mode, kv.second.stages);
     first = false;
   }
   fprintf(f, "\n}\n");
@@ -152,13 +178,13 @@ int gbdw_tune_load(const char* path) {
     const size_t end = text.find('"', pos + 1);
     if (end == std::string::npos) break;
     const std::string key = text.substr(pos + 1, end - pos - 1);
-    int gp, sp, LsE, epi, th, spt;
+    int gp, sp, LsE, epi, th, spt, mode = 0, stages = 4;
     const size_t lb = text.find('[', end);
     if (lb == std::string::npos) break;
     if (sscanf(key.c_str(), "g%d_s%d_L%d_e%d", &gp, &sp, &LsE, &epi) == 4 &&
-        sscanf(text.c_str() + lb, "[%d , %d]", &th, &spt) == 2 && th > 0 && th <= 256 && th % 32 == 0 &&
-        (spt == 1 || spt == 2 || spt == 4)) {
-      set_tuned_launch(gp, sp, LsE, epi, DhopLaunch{th, spt});
+        sscanf(text.c_str() + lb, "[%d , %d , %d , %d]", &th, &spt, &mode, &stages) >= 2 && th > 0 && th <= 256 &&
+        th % 32 == 0 && (spt == 1 || spt == 2 || spt == 4) && (mode == 0 || mode == 1) && (stages == 2 || stages == 4)) {
+      set_tuned_launch(gp, sp, LsE, epi, DhopLaunch{th, spt, mode, stages});
       ++loaded;
     }
     pos = text.find(']', lb);

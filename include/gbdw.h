@@ -39,7 +39,8 @@ typedef enum {
   GBDW_ERR_TABLE = 4,         /* neighbour table out of range */
   GBDW_ERR_NOT_CONVERGED = 5, /* solver hit its iteration limit */
   GBDW_ERR_DIVERGED = 6,      /* solver produced a non-finite or non-positive quantity */
-  GBDW_ERR_NO_DEVICE = 7      /* no CUDA device visible */
+  GBDW_ERR_NO_DEVICE = 7,     /* no CUDA device visible */
+  GBDW_ERR_TIMEOUT = 8        /* a bounded device-side wait expired (reported by gbdw_synchronize) */
 } gbdw_status;
 
 /* Storage precision of a field.  Arithmetic is FP64 for GBDW_F64 and FP32 otherwise. */
@@ -194,11 +195,12 @@ int gbdw_batch_info(const gbdw_batch* b, int64_t info[4]);
 int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag);
 int gbdw_tune_load(const char* path);
 int gbdw_tune_save(const char* path);
-/* Writes the chosen (threads per CTA, slices per thread) for a field into cfg[2]. */
-int gbdw_tune_query(const gbdw_gauge* g, const gbdw_field* in, int cfg[2]);
+/* Writes the chosen shape for a field into cfg[4]: threads per CTA, slices per thread,
+ * form (0 direct loads, 1 TMA-staged neighbour blocks) and stages of the staged form. */
+int gbdw_tune_query(const gbdw_gauge* g, const gbdw_field* in, int cfg[4]);
 /* Pins the shape for fields like `in` (threads a multiple of 32 up to 256; slices per thread
- * 1, 2 or 4 dividing Ls*nrhs, at most 2 for F64). */
-int gbdw_tune_set(const gbdw_gauge* g, const gbdw_field* in, int threads, int spt);
+ * 1, 2 or 4 dividing Ls*nrhs, at most 2 for F64; form 0/1; stages 2/4). */
+int gbdw_tune_set(const gbdw_gauge* g, const gbdw_field* in, int threads, int spt, int form, int stages);
 
 /* ------------------------------------------------------------------ timing on the library stream */
 typedef struct gbdw_timer gbdw_timer;
@@ -208,6 +210,11 @@ int gbdw_timer_stop(gbdw_timer* t, double* ms); /* synchronises, returns elapsed
 int gbdw_timer_destroy(gbdw_timer* t);
 /* Writes nbytes of junk through a scratch buffer to evict L2 (no-op if nbytes == 0). */
 int gbdw_flush_l2(size_t nbytes);
+
+/* Runs one CTA whose bounded mbarrier wait cannot complete (nothing is copied), so it expires
+ * after limit_ns (at most 0.1 s); the next gbdw_synchronize() then reports GBDW_ERR_TIMEOUT.
+ * Exercises the timeout path of the staged kernels without any fault. */
+int gbdw_selftest_wait_timeout(uint64_t limit_ns);
 
 /* Page-locked host memory for fast host<->device copies of reference-layout buffers. */
 int gbdw_host_alloc(size_t nbytes, void** ptr);

@@ -20,10 +20,13 @@ def test_norm_dot_axpby(gpu, prec, tol):
     x = gb.Field(lat, prec).load(c["phi"])
     y = gb.Field(lat, prec).load(d["phi"])
     xa, ya = x.numpy(), y.numpy()  # values as stored
-    assert abs(x.norm2() - np.sum(xa ** 2)) / np.sum(xa ** 2) < 1e-12
+    # F64 fields sum in FP64 throughout; F32/F16 fields sum each 24-real entry in FP32 and
+    # everything above the entry in FP64
+    sum_tol = 1e-12 if prec == gb.F64 else 1e-7
+    assert abs(x.norm2() - np.sum(xa ** 2)) / np.sum(xa ** 2) < sum_tol
     dt = x.dot(y)
     ref = np.vdot(_c(xa), _c(ya))
-    assert abs(dt - ref) / abs(ref) < 1e-10
+    assert abs(dt - ref) / abs(ref) < (1e-10 if prec == gb.F64 else 1e-5)
     y.axpby(0.5, x, -2.0)
     exp = 0.5 * xa - 2.0 * ya
     assert np.linalg.norm(y.numpy() - exp) / np.linalg.norm(exp) < tol

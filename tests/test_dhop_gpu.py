@@ -120,20 +120,31 @@ def test_table_out_of_range_is_rejected(gpu):
     assert e.value.status == 4
 
 
-@pytest.mark.parametrize("prec,spts", [(gb.F32, (1, 2, 4)), (gb.F64, (1, 2))])
+SHAPES = {gb.F32: [(0, s, 4) for s in (1, 2, 4)] + [(1, s, st) for s in (1, 2) for st in (2, 4)],
+          gb.F64: [(0, s, 4) for s in (1, 2)] + [(1, s, st) for s in (1, 2) for st in (2, 4)]}
+
+
+@pytest.mark.parametrize("prec", [gb.F32, gb.F64])
 @pytest.mark.parametrize("threads", [64, 128, 256])
-def test_every_launch_shape(gpu, prec, spts, threads):
-    c = make_case((4, 4, 4, 4), 8)
-    ref = oracle.dslash(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], 8)
-    lat = gb.Lattice.from_table(c["nbr"], c["prm"], c["nsite"], 8)
+@pytest.mark.parametrize("Ls", [8, 12])
+def test_every_launch_shape(gpu, prec, threads, Ls):
+    """Direct and TMA-staged forms, every compiled slice split and stage count, Dhop and
+    DhopDag, including a lattice whose site count is not a multiple of the CTA's sites."""
+    c = make_case((4, 6, 2, 3), Ls)
+    lat = gb.Lattice.from_table(c["nbr"], c["prm"], c["nsite"], Ls)
     g = gb.Gauge(lat, c["U"], prec)
     x = gb.Field(lat, prec).load(c["phi"])
     y = gb.Field(lat, prec)
-    for spt in spts:
-        gb.tune_set(g, x, threads, spt)
-        gb.dhop(g, y, x)
-        assert rel_err(y.numpy(), ref) < TOL[prec], (threads, spt)
-    gb.tune_set(g, x, 128, spts[-1] if prec == gb.F64 else 2)
+    for dag in (0, 1):
+        ref = oracle.dslash(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], Ls, dag)
+        for form, spt, stages in SHAPES[prec]:
+            if Ls % spt:
+                continue
+            gb.tune_set(g, x, threads, spt, form, stages)
+            y.zero()
+            gb.dhop(g, y, x, dag)
+            assert rel_err(y.numpy(), ref) < TOL[prec], (form, spt, stages, dag)
+    gb.synchronize()
 
 
 def test_periodic_lattice_equals_table_lattice(gpu):

@@ -60,15 +60,39 @@ def test_fp16_storage_dhop_and_m(gpu, gprec, tol, dag):
     assert e1 < tol and e2 < tol
 
 
-@pytest.mark.parametrize("spt", [1, 2, 4])
-def test_fp16_every_slice_split(gpu, spt):
-    c, lat, g, x = _setup((4, 4, 4, 4), 8, gb.F16, gb.F16)
+@pytest.mark.parametrize("form,spt,stages", [(0, 1, 4), (0, 2, 4), (0, 4, 4), (1, 2, 2), (1, 2, 4), (1, 4, 2),
+                                              (1, 4, 4)])
+@pytest.mark.parametrize("gprec", [gb.F16, gb.BF16])
+def test_fp16_every_shape(gpu, form, spt, stages, gprec):
+    c, lat, g, x = _setup((4, 2, 6, 2), 12, gb.F16, gprec)
     y = gb.Field(lat, gb.F16)
-    gb.tune_set(g, x, 128, spt)
-    gb.dwf_m(g, y, x, M5, MF, 0)
-    ref = oracle.dwf_m(c["U"], c["phi"], c["nbr"], c["nsite"], 8, M5, MF, 0)
-    assert rel_err(y.numpy(), ref) < 5e-3
-    gb.tune_set(g, x, 128, 4)
+    gb.tune_set(g, x, 128, spt, form, stages)
+    for dag in (0, 1):
+        n2 = gb.dwf_m(g, y, x, M5, MF, dag, want_norm=True)
+        ref = oracle.dwf_m(c["U"], c["phi"], c["nbr"], c["nsite"], 12, M5, MF, dag)
+        out = y.numpy()
+        assert rel_err(out, ref) < (5e-3 if gprec == gb.F16 else 3e-2)
+        assert abs(n2 - float(np.sum(out ** 2))) / n2 < 1e-5
+        gb.dhop(g, y, x, dag)
+        ref = oracle.dslash(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], 12, dag)
+        assert rel_err(y.numpy(), ref) < (5e-3 if gprec == gb.F16 else 3e-2)
+    gb.synchronize()
+
+
+@pytest.mark.parametrize("prec,tol", [(gb.F64, 1e-12), (gb.F32, 1e-6)])
+@pytest.mark.parametrize("stages", [2, 4])
+def test_staged_form_m_and_norm(gpu, prec, tol, stages):
+    c, lat, g, x = _setup((4, 4, 2, 4), 8, prec)
+    y = gb.Field(lat, prec)
+    for spt in (1, 2):
+        gb.tune_set(g, x, 128, spt, 1, stages)
+        for dag in (0, 1):
+            n2 = gb.dwf_m(g, y, x, M5, MF, dag, want_norm=True)
+            ref = oracle.dwf_m(c["U"], c["phi"], c["nbr"], c["nsite"], 8, M5, MF, dag)
+            out = y.numpy()
+            assert rel_err(out, ref) < tol
+            assert abs(n2 - float(np.sum(out ** 2))) / n2 < tol * 10
+    gb.synchronize()
 
 
 def test_fp16_roundtrip_precision(gpu):
