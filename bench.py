@@ -496,6 +496,38 @@ def run_reference(args, D: Dist) -> dict | None:
             "e2e": {"value": round(value, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+ONLY = {  # name -> (dims, Ls, spinor precision, gauge precision, dag)
+    "dhop_f32": (DIMS, LS, 1, 1, 0), "dhopdag_f32": (DIMS, LS, 1, 1, 1), "dhop_f64": (DIMS, LS, 0, 0, 0),
+    "dhop_f16": (DIMS, LS, 2, 2, 0), "dhop_bf16": (DIMS, LS, 2, 3, 0),
+}
+
+
+def run_only(args) -> dict:
+    """One hopping-term workload, nothing else: the command profiles are captured with.
+    --shape threads,slices,form,stages pins the launch shape (form 0 direct, 1 TMA-staged);
+    without it the autotuner picks."""
+    import gridbench_gb300 as gb
+    dims, Ls, sp, gp, dag = ONLY[args.only]
+    lat = gb.Lattice.periodic(dims, Ls)
+    g = gb.Gauge(lat, None, gp, seed=11)
+    xs = [gb.Field(lat, sp).gaussian(21 + i) for i in range(2)]
+    ys = [gb.Field(lat, sp) for _ in range(2)]
+    if args.shape:
+        th, spt, form, st = (int(v) for v in args.shape.split(","))
+        gb.tune_set(g, xs[0], th, spt, form, st)
+    else:
+        gb.tune_dhop(g, ys[0], xs[0], dag)
+    ms, launches = time_dhop(gb, g, list(zip(ys, xs)), args.steps, args.warmup, dag)
+    gb.synchronize()
+    V5 = int(np.prod(dims)) * Ls
+    t = ms / args.steps / 1e3
+    peak, _ = measured_peak_hbm()
+    return {"workload": args.only, "lattice": list(dims), "Ls": Ls, "steps": args.steps,
+            "us_per_launch": round(t * 1e6, 3), "gflops": round(FLOP_PER_SITE * V5 / t / 1e9, 1),
+            "hbm_frac": round(algo_bytes(sp, gp, Ls) * V5 / t / 1e9 / peak, 4),
+            "shape": list(gb.tune_query(g, xs[0])), "gpu_launches": int(launches)}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -509,9 +541,14 @@ def main(argv=None):
     ap.add_argument("--ref-seconds", type=float, default=30.0)
     ap.add_argument("--cg-small", action="store_true", help="CG secondary on 16^4 x 16 instead of 32^4 x 16")
     ap.add_argument("--cg-max-iter", type=int, default=20000)
+    ap.add_argument("--only", choices=sorted(ONLY), help="time one hopping-term workload only (for profiling)")
+    ap.add_argument("--shape", help="with --only: threads,slices_per_thread,form,stages")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
+    if args.only:
+        print(json.dumps(run_only(args)), flush=True)
+        return
     D = Dist()
     try:
         line = run_reference(args, D) if args.impl == "reference" else run_ours(args, D)

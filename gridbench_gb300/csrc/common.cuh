@@ -29,6 +29,7 @@ void* scratch(size_t bytes, int slot);
 int ensure_device();
 int num_sms();
 unsigned* device_error_word();  // set by kernels whose bounded waits expired
+size_t max_dynamic_smem();      // opt-in dynamic shared memory per CTA, minus room for static
 
 #define GBDW_CUDA(call)                                       \
   do {                                                        \

@@ -30,6 +30,9 @@ double* g_pinned = nullptr;
 void set_error(const std::string& msg) { g_error = msg; }
 
 int cuda_fail(cudaError_t e, const char* what) {
+  // clear the runtime's record of a non-sticky error so the next launch check does not
+  // report it again
+  cudaGetLastError();
   char buf[512];
   snprintf(buf, sizeof buf, "CUDA error in %s: %s", what, cudaGetErrorString(e));
   g_error = buf;
@@ -58,6 +61,21 @@ int ensure_device() {
 }
 
 int num_sms() { return g_num_sms > 0 ? g_num_sms : 152; }
+
+size_t max_dynamic_smem() {
+  static size_t v = 0;
+  if (!v) {
+    int dev = 0, optin = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess && optin > 0)
+      v = size_t(optin);
+    else
+      v = 227 * 1024;
+    cudaGetLastError();
+  }
+  // keep 1 KB for the kernels' static shared memory (reduction scratch, barriers)
+  return v - 1024;
+}
 
 cudaStream_t stream() { return g_have_user_stream ? g_user_stream : g_own_stream; }
 

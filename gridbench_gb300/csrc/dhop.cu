@@ -111,8 +111,9 @@ bool tma_shape(int prec, int LsE, DhopLaunch L, int* NS, int* threads, size_t* s
   if (round32(ns * Tps) > 256) return false;
   const size_t esz = spinor_elem_bytes(prec);
   const size_t stage = size_t(ns) * (12 * size_t(LsE) * esz + (prec == GBDW_F16 ? 4 * size_t(LsE) : 0));
-  const size_t sm = size_t(L.stages) * stage + size_t(L.stages) * 8;
-  if (sm > 227 * 1024) return false;
+  const size_t links = size_t(ns) * 8 * link_bytes(prec == GBDW_F16 ? GBDW_F16 : prec);
+  const size_t sm = size_t(L.stages) * stage + links + size_t(L.stages + 1) * 8;
+  if (sm > max_dynamic_smem()) return false;
   *NS = ns;
   *threads = round32(ns * Tps);
   *smem = sm;

@@ -26,7 +26,10 @@ int go_tma(const DhopParams& p, DhopLaunch L) {
   auto kern = k_dhop_tma<PIN, POUT, GP, DAG, N, EPI, STAGES>;
   static bool opted_in = false;  // one attribute call per instance
   if (!opted_in) {
-    GBDW_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    cudaFuncAttributes fa;
+    GBDW_CUDA(cudaFuncGetAttributes(&fa, kern));
+    const size_t limit = max_dynamic_smem() + 1024 - fa.sharedSizeBytes;
+    GBDW_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(limit)));
     opted_in = true;
   }
   const unsigned blocks = unsigned((p.nsite + NS - 1) / NS);

@@ -105,13 +105,56 @@ __device__ __forceinline__ void lds(const unsigned char* base, int e, cpx<typena
   }
 }
 
-// One leg from a staged neighbour block (blk: the 12*LsE entries, nrm: its norms for F16).
+// A site's 8 doubled links in shared memory (staged as one block per site).
+template <int GP>
+struct LinkSmem;
+template <>
+struct LinkSmem<GBDW_F32> {
+  static constexpr unsigned bytes = 8 * 72;
+  static __device__ __forceinline__ void load(const unsigned char* site_links, int L, cpx<float> (&u)[3][3]) {
+    const float2* p = reinterpret_cast<const float2*>(site_links) + L * 9;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) u[k / 3][k % 3] = {p[k].x, p[k].y};
+  }
+};
+template <>
+struct LinkSmem<GBDW_F64> {
+  static constexpr unsigned bytes = 8 * 144;
+  static __device__ __forceinline__ void load(const unsigned char* site_links, int L, cpx<double> (&u)[3][3]) {
+    const double2* p = reinterpret_cast<const double2*>(site_links) + L * 9;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) u[k / 3][k % 3] = {p[k].x, p[k].y};
+  }
+};
+template <>
+struct LinkSmem<GBDW_F16> {
+  static constexpr unsigned bytes = 8 * 24;
+  static __device__ __forceinline__ void load(const unsigned char* site_links, int L, cpx<float> (&u)[3][3]) {
+    const unsigned* p = reinterpret_cast<const unsigned*>(site_links) + L * 6;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) u[k / 3][k % 3] = h2c(p[k]);
+    third_row(u);
+  }
+};
+template <>
+struct LinkSmem<GBDW_BF16> {
+  static constexpr unsigned bytes = 8 * 24;
+  static __device__ __forceinline__ void load(const unsigned char* site_links, int L, cpx<float> (&u)[3][3]) {
+    const unsigned* p = reinterpret_cast<const unsigned*>(site_links) + L * 6;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) u[k / 3][k % 3] = b2c(p[k]);
+    third_row(u);
+  }
+};
+
+// One leg from a staged neighbour block (blk: the 12*LsE entries, nrm: its norms for F16)
+// with the site's staged links.
 template <int PIN, int GP, int DAG, int N, int L, class T>
-__device__ __forceinline__ void hop_leg_smem(const void* __restrict__ U, size_t link, const unsigned char* blk,
+__device__ __forceinline__ void hop_leg_smem(const unsigned char* site_links, const unsigned char* blk,
                                              const float* nrm, int s0, int LsE, cpx<T> (&acc)[N][12]) {
   using S = LegSpin<DAG ? (L ^ 4) : L>;
   cpx<T> u[3][3];
-  LinkIO<GP>::load(U, link, u);
+  LinkSmem<GP>::load(site_links, L, u);
   cpx<T> h0[N][3], h1[N][3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
@@ -165,14 +208,9 @@ __device__ __forceinline__ void hop_leg_smem(const void* __restrict__ U, size_t 
   }
 }
 
-// Dynamic shared memory of the staged kernel for NS sites.
-template <int PIN>
-__host__ __device__ inline unsigned tma_stage_bytes(int NS, int LsE) {
-  const unsigned blk = 12u * unsigned(LsE) * ESz<PIN>::v;
-  const unsigned nb = (PIN == GBDW_F16) ? 4u * unsigned(LsE) : 0u;
-  return unsigned(NS) * (blk + nb);
-}
 
+// Shared memory: STAGES rings of NS neighbour blocks (+ norms), then the NS sites' links,
+// then STAGES+1 mbarriers (the last one for the links).
 template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int STAGES>
 __global__ void __launch_bounds__(256) k_dhop_tma(const DhopParams p, int NS) {
   using T = typename Arith<PIN>::T;
@@ -182,7 +220,8 @@ __global__ void __launch_bounds__(256) k_dhop_tma(const DhopParams p, int NS) {
   const unsigned blk = 12u * unsigned(LsE) * ESz<PIN>::v;
   const unsigned nblk = (PIN == GBDW_F16) ? 4u * unsigned(LsE) : 0u;
   const unsigned stage = unsigned(NS) * (blk + nblk);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * stage);
+  unsigned char* links = smem + STAGES * stage;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(links + NS * LinkSmem<GP>::bytes);
   const int tid = threadIdx.x;
   const int64_t site0 = int64_t(blockIdx.x) * NS;
   const int nvalid = int(min(int64_t(NS), p.nsite - site0));
@@ -193,21 +232,36 @@ __global__ void __launch_bounds__(256) k_dhop_tma(const DhopParams p, int NS) {
 
   if (tid == 0) {
 #pragma unroll
-    for (int s = 0; s < STAGES; ++s) mbar_init(&bars[s], 1);
+    for (int s = 0; s <= STAGES; ++s) mbar_init(&bars[s], 1);
     fence_mbar_init();
+  }
+  // the issuing threads keep their site's 8 neighbours in registers
+  uint32_t nb[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (tid < nvalid) {
+    const uint4* q = reinterpret_cast<const uint4*>(p.nbr4 + (site0 + tid) * 8);
+    const uint4 a = __ldg(q), b = __ldg(q + 1);
+    nb[0] = a.x; nb[1] = a.y; nb[2] = a.z; nb[3] = a.w;
+    nb[4] = b.x; nb[5] = b.y; nb[6] = b.z; nb[7] = b.w;
   }
   __syncthreads();
 
   auto issue = [&](int L, int st) {
     unsigned char* base = smem + st * stage;
     if (tid < nvalid) {
-      const int64_t n = __ldg(p.nbr4 + (site0 + tid) * 8 + L);
+      const int64_t n = nb[L];
       bulk_g2s(base + tid * blk, (const unsigned char*)p.in + n * blk, blk, &bars[st]);
       if constexpr (PIN == GBDW_F16)
         bulk_g2s(base + NS * blk + tid * nblk, (const unsigned char*)p.in_norm + n * nblk, nblk, &bars[st]);
     }
     if (tid == 0) mbar_arrive_expect_tx(&bars[st], expect);
   };
+
+  // links of the CTA's sites: one block of 8 links per site
+  if (tid < nvalid)
+    bulk_g2s(links + tid * LinkSmem<GP>::bytes,
+             (const unsigned char*)p.U + (site0 + tid) * int64_t(LinkSmem<GP>::bytes), LinkSmem<GP>::bytes,
+             &bars[STAGES]);
+  if (tid == 0) mbar_arrive_expect_tx(&bars[STAGES], unsigned(nvalid) * LinkSmem<GP>::bytes);
 
 #pragma unroll
   for (int L = 0; L < STAGES && L < 8; ++L) issue(L, L);
@@ -218,9 +272,9 @@ __global__ void __launch_bounds__(256) k_dhop_tma(const DhopParams p, int NS) {
 #pragma unroll
     for (int k = 0; k < 12; ++k) acc[j][k] = {T(0), T(0)};
 
-  const size_t link0 = size_t(site0 + (active ? sl : 0)) * 8;
   int consumed = 0;  // legs whose stage has been waited for
-  bool failed = false;
+  bool failed = __syncthreads_or(!mbar_wait_bounded(&bars[STAGES], 0, kWaitLimitNs));
+  const unsigned char* my_links = links + (active ? sl : 0) * LinkSmem<GP>::bytes;
 #define GBDW_TMA_LEG(L)                                                                                     \
   if (!failed) {                                                                                            \
     const int st = (L) % STAGES;                                                                            \
@@ -230,7 +284,7 @@ __global__ void __launch_bounds__(256) k_dhop_tma(const DhopParams p, int NS) {
       consumed = (L) + 1;                                                                                   \
       const unsigned char* base = smem + st * stage;                                                        \
       if (active)                                                                                           \
-        hop_leg_smem<PIN, GP, DAG, N, L>(p.U, link0 + (L), base + sl * blk,                                 \
+        hop_leg_smem<PIN, GP, DAG, N, L>(my_links, base + sl * blk,                                          \
                                          reinterpret_cast<const float*>(base + NS * blk + sl * nblk), s0,   \
                                          LsE, acc);                                                         \
       if ((L) + STAGES < 8) {                                                                               \
@@ -248,6 +302,7 @@ __global__ void __launch_bounds__(256) k_dhop_tma(const DhopParams p, int NS) {
     // drain every stage that still has copies in flight before the CTA's smem is released
     const int issued = min(8, consumed + STAGES);
     for (int L = consumed; L < issued; ++L) mbar_wait_bounded(&bars[L % STAGES], (L / STAGES) & 1, kWaitLimitNs);
+    mbar_wait_bounded(&bars[STAGES], 0, kWaitLimitNs);  // the link copies
   }
   float part = 0.f;
   double dpart = 0.0;

@@ -140,7 +140,11 @@ def test_every_launch_shape(gpu, prec, threads, Ls):
         for form, spt, stages in SHAPES[prec]:
             if Ls % spt:
                 continue
-            gb.tune_set(g, x, threads, spt, form, stages)
+            try:
+                gb.tune_set(g, x, threads, spt, form, stages)
+            except gb.GbdwError:
+                assert form == 1  # a staged ring that does not fit in shared memory
+                continue
             y.zero()
             gb.dhop(g, y, x, dag)
             assert rel_err(y.numpy(), ref) < TOL[prec], (form, spt, stages, dag)
