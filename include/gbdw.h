@@ -216,6 +216,17 @@ int gbdw_flush_l2(size_t nbytes);
  * Exercises the timeout path of the staged kernels without any fault. */
 int gbdw_selftest_wait_timeout(uint64_t limit_ns);
 
+/* Sum of |x_i|^2 in FP64 over n complex numbers (re, im interleaved; prec GBDW_F64 or
+ * GBDW_F32) in device memory the caller owns, written to *result (host).  For callers that
+ * cannot allocate device memory -- programs whose own pool allocator owns the GPU, solver
+ * loops that must not pay cudaMalloc's latency -- it allocates nothing: its partial sums live
+ * in a fixed 8 KB device array that every GPU loading the library keeps until exit.  No
+ * counterpart in the reference.  Limit: n <= 2^24 (larger n returns GBDW_ERR_INVALID).  All
+ * calls share that array, so calls that overlap on the GPU race; calls in one stream do not.
+ * The first call on each device looks the array up (cudaGetSymbolAddress): make it before
+ * any stream capture. */
+int gbdw_norm2_noalloc(const void* x, int prec, uint64_t n, double* result);
+
 /* Page-locked host memory for fast host<->device copies of reference-layout buffers. */
 int gbdw_host_alloc(size_t nbytes, void** ptr);
 int gbdw_host_free(void* ptr);
