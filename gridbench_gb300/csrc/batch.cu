@@ -34,7 +34,7 @@ __device__ __forceinline__ void batch_thread(const DhopParams& p, unsigned tid) 
   using T = typename Arith<PIN>::T;
   cpx<T> acc[N][12];
   dhop_thread<PIN, GP, DAG, N>(p, site, s0, acc);
-  store_spinor<PIN, N>(p.out, p.out_norm, int64_t(site) * 12 * p.LsE + s0, int64_t(site) * p.LsE + s0, p.LsE, acc);
+  store_spinor<PIN, N>(p.out, p.out_norm, site, s0, p.LsE, p.LsP, acc);
 }
 
 template <int DAG>
@@ -145,11 +145,13 @@ int build(gbdw_batch* b) {
     p.nbr5 = nullptr;
     p.nsite = g->lat->nsite;
     p.LsE = x->LsE;
+    p.LsP = x->LsP;
     p.Ls = g->lat->Ls;
     p.a5 = p.mf = 0.0;
     p.partials = nullptr;
     p.counter = nullptr;
     p.result = nullptr;
+    p.err = nullptr;
     I.nthreads = unsigned(p.nsite * (p.LsE / spt));
     I.item_begin = items;
     items += (I.nthreads + b->threads - 1) / b->threads;

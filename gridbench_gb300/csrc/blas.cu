@@ -6,6 +6,9 @@
 // the fixed-order grid reduction of common.cuh.
 #include "blas.h"
 #include "common.cuh"
+#include "layout.cuh"
+
+#include <type_traits>
 
 namespace gbdw {
 
@@ -21,52 +24,21 @@ struct Calc<GBDW_F64> {
 };
 
 template <int P, class T>
-__device__ __forceinline__ void ld24(const void* d, const float* nrm, int64_t site, int e, int LsE, T (&v)[24]) {
-  const int64_t b = site * 12 * LsE + e;
-  if (P == GBDW_F64) {
+__device__ __forceinline__ void ld24(const void* d, const float* nrm, int64_t site, int e, int LsE, int LsP, T (&v)[24]) {
+  const float n = (P == GBDW_F16) ? __ldg(nrm + site * LsE + e) : 1.f;
 #pragma unroll
-    for (int k = 0; k < 12; ++k) {
-      const double2 a = __ldg((const double2*)d + b + int64_t(k) * LsE);
-      v[2 * k] = T(a.x);
-      v[2 * k + 1] = T(a.y);
-    }
-  } else if (P == GBDW_F32) {
-#pragma unroll
-    for (int k = 0; k < 12; ++k) {
-      const float2 a = __ldg((const float2*)d + b + int64_t(k) * LsE);
-      v[2 * k] = T(a.x);
-      v[2 * k + 1] = T(a.y);
-    }
-  } else {
-    const float n = __ldg(nrm + site * LsE + e);
-#pragma unroll
-    for (int k = 0; k < 12; ++k) {
-      const float2 a = __half22float2(__ldg((const __half2*)d + b + int64_t(k) * LsE));
-      v[2 * k] = T(a.x * n);
-      v[2 * k + 1] = T(a.y * n);
-    }
+  for (int k = 0; k < 12; ++k) {
+    const auto a = Elem<P>::ld(d, site * 12 + k, e, LsP);
+    v[2 * k] = (P == GBDW_F16) ? T(float(a.r) * n) : T(a.r);
+    v[2 * k + 1] = (P == GBDW_F16) ? T(float(a.i) * n) : T(a.i);
   }
 }
 
 // Stores v and returns the entry's |.|^2 as stored.
 template <int P, class T>
-__device__ __forceinline__ T st24(void* d, float* nrm, int64_t site, int e, int LsE, const T (&v)[24]) {
-  const int64_t b = site * 12 * LsE + e;
+__device__ __forceinline__ T st24(void* d, float* nrm, int64_t site, int e, int LsE, int LsP, const T (&v)[24]) {
   T s = T(0);
-  if (P == GBDW_F64) {
-#pragma unroll
-    for (int k = 0; k < 12; ++k) {
-      ((double2*)d)[b + int64_t(k) * LsE] = make_double2(double(v[2 * k]), double(v[2 * k + 1]));
-      s += v[2 * k] * v[2 * k] + v[2 * k + 1] * v[2 * k + 1];
-    }
-  } else if (P == GBDW_F32) {
-#pragma unroll
-    for (int k = 0; k < 12; ++k) {
-      const float re = float(v[2 * k]), im = float(v[2 * k + 1]);
-      ((float2*)d)[b + int64_t(k) * LsE] = make_float2(re, im);
-      s += T(re * re + im * im);
-    }
-  } else {
+  if constexpr (P == GBDW_F16) {
     float m = 0.f;
 #pragma unroll
     for (int k = 0; k < 24; ++k) m = fmaxf(m, fabsf(float(v[k])));
@@ -74,10 +46,17 @@ __device__ __forceinline__ T st24(void* d, float* nrm, int64_t site, int e, int 
     nrm[site * LsE + e] = m;
 #pragma unroll
     for (int k = 0; k < 12; ++k) {
-      const __half2 h = __floats2half2_rn(float(v[2 * k]) * sc, float(v[2 * k + 1]) * sc);
-      ((__half2*)d)[b + int64_t(k) * LsE] = h;
-      const float2 f = __half22float2(h);
+      const float2 f = __half22float2(__floats2half2_rn(float(v[2 * k]) * sc, float(v[2 * k + 1]) * sc));
+      Elem<GBDW_F16>::st(d, site * 12 + k, e, LsP, f.x, f.y);
       s += T((f.x * f.x + f.y * f.y) * m * m);
+    }
+  } else {
+    using S = typename std::conditional<P == GBDW_F64, double, float>::type;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      const S re = S(v[2 * k]), im = S(v[2 * k + 1]);
+      Elem<P>::st(d, site * 12 + k, e, LsP, re, im);
+      s += T(re) * T(re) + T(im) * T(im);
     }
   }
   return s;
@@ -86,10 +65,12 @@ __device__ __forceinline__ T st24(void* d, float* nrm, int64_t site, int e, int 
 struct FieldRef {
   const void* d;
   const float* n;
+  int LsP;
 };
 struct FieldOut {
   void* d;
   float* n;
+  int LsP;
 };
 
 template <int P>
@@ -101,7 +82,7 @@ __global__ void k_norm2(FieldRef x, int64_t nsite, int LsE, Reduce red) {
     const int64_t site = i / LsE;
     const int e = int(i - site * LsE);
     T v[24];
-    ld24<P>(x.d, x.n, site, e, LsE, v);
+    ld24<P>(x.d, x.n, site, e, LsE, x.LsP, v);
     T s = T(0);
 #pragma unroll
     for (int k = 0; k < 24; ++k) s += v[k] * v[k];
@@ -119,8 +100,8 @@ __global__ void k_dot(FieldRef x, FieldRef y, int64_t nsite, int LsE, Reduce red
     const int64_t site = i / LsE;
     const int e = int(i - site * LsE);
     T a[24], b[24];
-    ld24<PX>(x.d, x.n, site, e, LsE, a);
-    ld24<PY>(y.d, y.n, site, e, LsE, b);
+    ld24<PX>(x.d, x.n, site, e, LsE, x.LsP, a);
+    ld24<PY>(y.d, y.n, site, e, LsE, y.LsP, b);
     T re = T(0), im = T(0);
 #pragma unroll
     for (int k = 0; k < 12; ++k) {
@@ -142,11 +123,11 @@ __global__ void k_axpby(double a, FieldRef x, double b, FieldOut y, int64_t nsit
     const int64_t site = i / LsE;
     const int e = int(i - site * LsE);
     T u[24], v[24];
-    ld24<PX>(x.d, x.n, site, e, LsE, u);
-    ld24<PY>(y.d, y.n, site, e, LsE, v);
+    ld24<PX>(x.d, x.n, site, e, LsE, x.LsP, u);
+    ld24<PY>(y.d, y.n, site, e, LsE, y.LsP, v);
 #pragma unroll
     for (int k = 0; k < 24; ++k) v[k] = T(a) * u[k] + T(b) * v[k];
-    st24<PY>(y.d, y.n, site, e, LsE, v);
+    st24<PY>(y.d, y.n, site, e, LsE, y.LsP, v);
   }
 }
 
@@ -160,11 +141,11 @@ __global__ void k_xmy_norm(FieldRef b, FieldRef t, FieldOut r, int64_t nsite, in
     const int64_t site = i / LsE;
     const int e = int(i - site * LsE);
     T u[24], v[24];
-    ld24<PB>(b.d, b.n, site, e, LsE, u);
-    ld24<PT>(t.d, t.n, site, e, LsE, v);
+    ld24<PB>(b.d, b.n, site, e, LsE, b.LsP, u);
+    ld24<PT>(t.d, t.n, site, e, LsE, t.LsP, v);
 #pragma unroll
     for (int k = 0; k < 24; ++k) u[k] -= v[k];
-    acc[0] += double(st24<PR>(r.d, r.n, site, e, LsE, u));
+    acc[0] += double(st24<PR>(r.d, r.n, site, e, LsE, r.LsP, u));
   }
   grid_sum<1>(acc, red.partials, red.counter, red.result);
 }
@@ -181,16 +162,16 @@ __global__ void k_cg_xr(double alpha, FieldOut x, FieldRef p, FieldOut r, FieldR
     const int64_t site = i / LsE;
     const int e = int(i - site * LsE);
     T u[24], v[24];
-    ld24<PX>(x.d, x.n, site, e, LsE, u);
-    ld24<PP>(p.d, p.n, site, e, LsE, v);
+    ld24<PX>(x.d, x.n, site, e, LsE, x.LsP, u);
+    ld24<PP>(p.d, p.n, site, e, LsE, p.LsP, v);
 #pragma unroll
     for (int k = 0; k < 24; ++k) u[k] += al * v[k];
-    st24<PX>(x.d, x.n, site, e, LsE, u);
-    ld24<PR>(r.d, r.n, site, e, LsE, u);
-    ld24<PA>(ap.d, ap.n, site, e, LsE, v);
+    st24<PX>(x.d, x.n, site, e, LsE, x.LsP, u);
+    ld24<PR>(r.d, r.n, site, e, LsE, r.LsP, u);
+    ld24<PA>(ap.d, ap.n, site, e, LsE, ap.LsP, v);
 #pragma unroll
     for (int k = 0; k < 24; ++k) u[k] -= al * v[k];
-    acc[0] += double(st24<PR>(r.d, r.n, site, e, LsE, u));
+    acc[0] += double(st24<PR>(r.d, r.n, site, e, LsE, r.LsP, u));
   }
   grid_sum<1>(acc, red.partials, red.counter, red.result);
 }
@@ -205,17 +186,17 @@ __global__ void k_cg_p(double beta, FieldRef r, FieldOut p, FieldOut q, int64_t 
     const int64_t site = i / LsE;
     const int e = int(i - site * LsE);
     T u[24], v[24];
-    ld24<PR>(r.d, r.n, site, e, LsE, u);
-    ld24<PP>(p.d, p.n, site, e, LsE, v);
+    ld24<PR>(r.d, r.n, site, e, LsE, r.LsP, u);
+    ld24<PP>(p.d, p.n, site, e, LsE, p.LsP, v);
 #pragma unroll
     for (int k = 0; k < 24; ++k) v[k] = u[k] + be * v[k];
-    st24<PP>(p.d, p.n, site, e, LsE, v);
-    if (PQ >= 0) st24<PQ < 0 ? GBDW_F32 : PQ>(q.d, q.n, site, e, LsE, v);
+    st24<PP>(p.d, p.n, site, e, LsE, p.LsP, v);
+    if (PQ >= 0) st24<PQ < 0 ? GBDW_F32 : PQ>(q.d, q.n, site, e, LsE, q.LsP, v);
   }
 }
 
-FieldRef ref(const gbdw_field* f) { return FieldRef{f->d, f->norm}; }
-FieldOut out(gbdw_field* f) { return FieldOut{f->d, f->norm}; }
+FieldRef ref(const gbdw_field* f) { return FieldRef{f->d, f->norm, f->LsP}; }
+FieldOut out(gbdw_field* f) { return FieldOut{f->d, f->norm, f->LsP}; }
 
 constexpr int kThreads = 256;
 int64_t grid_for(const gbdw_field* f) {
@@ -294,7 +275,7 @@ int blas_cg_p(double beta, const gbdw_field* r, gbdw_field* p, gbdw_field* q) {
   const int64_t ns = r->lat->nsite;
   const int L = r->LsE;
   const int qp = q ? q->prec : -1;
-  FieldOut qo = q ? out(q) : FieldOut{nullptr, nullptr};
+  FieldOut qo = q ? out(q) : FieldOut{nullptr, nullptr, 0};
   const int key = (r->prec * 4 + p->prec) * 8 + (qp + 1);
 #define GBDW_P(PR, PP, PQ)                                                                             \
   case (PR * 4 + PP) * 8 + (PQ + 1):                                                                   \

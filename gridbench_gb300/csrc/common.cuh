@@ -2,8 +2,9 @@
 //
 // Device layout ("GB300 layout"), chosen so that consecutive threads read consecutive
 // addresses and one 4D link serves every fifth-dimension slice of its site:
-//   spinor  [site][sc = spin*3+colour][e = s*nrhs + rhs]   complex (F64 16 B, F32 8 B, F16 4 B)
-//           F16 adds norm[site][e] (FP32, max |re|,|im| over the 24 reals of that 5D site)
+//   spinor  [site][sc = spin*3+colour][e = s*nrhs + rhs]   complex (F64 16 B, F32 8 B, F16 4 B);
+//           F32/F16 store slice pairs as (Re, Re, Im, Im) -- layout.cuh has the addressing --
+//           and F16 adds norm[site][e] (FP32, max |re|,|im| over the 24 reals of that 5D site)
 //   gauge   [site][mu][row][col] complex, 9 entries (F64/F32) or rows 0-1 only (F16/BF16)
 //   nbr4    [site][mu] uint32 neighbour 4D site (fast path)
 // "site" runs over 4D sites with SIMD lanes unrolled: site = outer_site*nsimd + lane, so a
@@ -68,10 +69,11 @@ struct gbdw_field {
   int prec;
   int nrhs;
   int LsE;           // Ls * nrhs, the innermost extent
+  int LsP;           // stored slots per row: LsE, rounded up to even for F32/F16
   void* d;           // complex data
   float* norm;       // F16 only
   size_t bytes;
-  int64_t elems() const { return lat->nsite * 12 * int64_t(LsE); }  // complex entries
+  int64_t elems() const { return lat->nsite * 12 * int64_t(LsP); }  // stored complex slots
 };
 
 namespace gbdw {

@@ -1,6 +1,7 @@
 // Operator entry points: Dhop / DhopDag, the Shamir operator M / M^dagger and M^dagger M.
 #include "common.cuh"
 #include "dhop_kernel.cuh"
+#include "layout.cuh"
 #include "tune.h"
 
 namespace gbdw {
@@ -50,6 +51,7 @@ DhopParams make_params(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* i
   p.nbr5 = g->lat->nbr5;
   p.nsite = g->lat->nsite;
   p.LsE = in->LsE;
+  p.LsP = in->LsP;
   p.Ls = g->lat->Ls;
   p.a5 = 0.0;
   p.mf = 0.0;
@@ -81,9 +83,9 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
   if (in->LsE % L.spt != 0) L.spt = 1;
   int NS = 0, tthreads = 0;
   size_t smem = 0;
-  if (L.mode == 1 && !tma_shape(in->prec, in->LsE, L, &NS, &tthreads, &smem)) L.mode = 0;
+  if (L.mode != 0 && !tma_shape(in->prec, in->LsE, L, &NS, &tthreads, &smem)) L.mode = 0;
   const int64_t nthreads = p.nsite * (p.LsE / L.spt);
-  const int64_t blocks = L.mode == 1 ? (p.nsite + NS - 1) / NS : (nthreads + L.threads - 1) / L.threads;
+  const int64_t blocks = L.mode != 0 ? (p.nsite + NS - 1) / NS : (nthreads + L.threads - 1) / L.threads;
   Reduce red;
   if (norm2) {
     if (int st = reduce_scratch(blocks, 1, &red)) return st;
@@ -104,15 +106,26 @@ bool tma_shape(int prec, int LsE, DhopLaunch L, int* NS, int* threads, size_t* s
   if (L.spt < 1 || LsE % L.spt != 0) return false;
   if (prec == GBDW_F16 && LsE % 4 != 0) return false;  // the norm block must be a 16-byte multiple
   const int Tps = LsE / L.spt;
+  const size_t esz = spinor_elem_bytes(prec);
+  const size_t blk = 12 * size_t(padded_slices(prec, LsE)) * esz + (prec == GBDW_F16 ? 4 * size_t(LsE) : 0);
+  const size_t lb = 8 * link_bytes(prec);
+  if (L.mode == 2) {
+    // one ring per warp: a warp owns 32/Tps whole sites
+    if (Tps > 32 || L.threads % 32 != 0 || L.threads > 256) return false;
+    const int nsw = 32 / Tps, W = L.threads / 32;
+    const size_t per_warp = size_t(L.stages) * nsw * blk + nsw * lb + ((size_t(L.stages + 1) * 8 + 15) & ~size_t(15));
+    if (W * per_warp > max_dynamic_smem()) return false;
+    *NS = W * nsw;
+    *threads = L.threads;
+    *smem = W * per_warp;
+    return true;
+  }
   if (Tps > 256) return false;
   int ns = L.threads / Tps > 1 ? L.threads / Tps : 1;
   auto round32 = [](int t) { return (t + 31) / 32 * 32; };  // whole warps (grid_sum shuffles)
   while (ns > 1 && round32(ns * Tps) > 256) --ns;
   if (round32(ns * Tps) > 256) return false;
-  const size_t esz = spinor_elem_bytes(prec);
-  const size_t stage = size_t(ns) * (12 * size_t(LsE) * esz + (prec == GBDW_F16 ? 4 * size_t(LsE) : 0));
-  const size_t links = size_t(ns) * 8 * link_bytes(prec == GBDW_F16 ? GBDW_F16 : prec);
-  const size_t sm = size_t(L.stages) * stage + links + size_t(L.stages + 1) * 8;
+  const size_t sm = size_t(L.stages) * ns * blk + size_t(ns) * lb + size_t(L.stages + 1) * 8;
   if (sm > max_dynamic_smem()) return false;
   *NS = ns;
   *threads = round32(ns * Tps);

@@ -1,5 +1,5 @@
 // The domain-wall Wilson hopping kernel (Dhop / DhopDag, optionally fused into the Shamir
-// operator M) for the GB300 layout described in common.cuh.
+// operator M) for the GB300 layout of layout.cuh.
 //
 // Maths per 5D site (WilsonKernelsHandCpu.h:94-303, applied per leg at :435-442, scalar form
 // dslash_simple.h:39-145): for each of the 8 legs, project the neighbour spinor to two
@@ -11,16 +11,19 @@
 // DhopDag = gamma5 Dhop gamma5 swaps every leg's spin structure with its opposite-sign
 // partner while keeping the leg's neighbour and link.
 //
-// Work decomposition: one thread per (4D site, SPT consecutive innermost slices).  The 4D
-// neighbour and the link of a leg are loaded once per thread and reused over its SPT slices;
-// threads of one site read the same link (one broadcast transaction) and consecutive threads
-// read consecutive slices, so each spinor component load of a warp is a run of whole sectors.
+// Work decomposition: one thread per (4D site, N consecutive slices).  The 4D neighbour and
+// the link of a leg are loaded once per thread and reused over its N slices; threads of one
+// site read the same link (one broadcast transaction) and consecutive threads read
+// consecutive slices, so each spinor component load of a warp is a run of whole sectors.
+// FP32/FP16 with an even N run the arithmetic on slice pairs with packed FFMA2/FADD2/FMUL2.
 #pragma once
+#include <type_traits>
+
 #include "common.cuh"
+#include "layout.cuh"
 
 namespace gbdw {
 
-// ------------------------------------------------------------------ storage traits
 template <int P>
 struct Arith {
   using T = float;
@@ -30,101 +33,11 @@ struct Arith<GBDW_F64> {
   using T = double;
 };
 
-// Load / store N consecutive complex entries starting at element e (e % N == 0).
-template <int P, int N>
-struct SpinIO;
-
-template <int N>
-struct SpinIO<GBDW_F32, N> {
-  static __device__ __forceinline__ void load(const void* base, int64_t e, cpx<float> (&v)[N]) {
-    if (N == 1) {
-      const float2 a = __ldg((const float2*)base + e);
-      v[0] = {a.x, a.y};
-    } else {
-#pragma unroll
-      for (int k = 0; k < N / 2; ++k) {
-        const float4 a = __ldg((const float4*)base + (e >> 1) + k);
-        v[2 * k] = {a.x, a.y};
-        v[2 * k + 1] = {a.z, a.w};
-      }
-    }
-  }
-  static __device__ __forceinline__ void store(void* base, int64_t e, const cpx<float> (&v)[N]) {
-    if (N == 1) {
-      ((float2*)base)[e] = make_float2(v[0].r, v[0].i);
-    } else {
-#pragma unroll
-      for (int k = 0; k < N / 2; ++k)
-        ((float4*)base)[(e >> 1) + k] = make_float4(v[2 * k].r, v[2 * k].i, v[2 * k + 1].r, v[2 * k + 1].i);
-    }
-  }
-};
-
-template <int N>
-struct SpinIO<GBDW_F64, N> {
-  static __device__ __forceinline__ void load(const void* base, int64_t e, cpx<double> (&v)[N]) {
-#pragma unroll
-    for (int k = 0; k < N; ++k) {
-      const double2 a = __ldg((const double2*)base + e + k);
-      v[k] = {a.x, a.y};
-    }
-  }
-  static __device__ __forceinline__ void store(void* base, int64_t e, const cpx<double> (&v)[N]) {
-#pragma unroll
-    for (int k = 0; k < N; ++k) ((double2*)base)[e + k] = make_double2(v[k].r, v[k].i);
-  }
-};
-
-__device__ __forceinline__ cpx<float> h2c(unsigned w) {
-  __half2 h = *reinterpret_cast<__half2*>(&w);
-  const float2 f = __half22float2(h);
-  return {f.x, f.y};
-}
-__device__ __forceinline__ unsigned c2h(float r, float i) {
-  __half2 h = __floats2half2_rn(r, i);
-  return *reinterpret_cast<unsigned*>(&h);
-}
-
-// F16 entries are stored divided by the site norm; load returns the stored values, the
-// caller multiplies by the norm (after projection, which is linear).
-template <int N>
-struct SpinIO<GBDW_F16, N> {
-  static __device__ __forceinline__ void load(const void* base, int64_t e, cpx<float> (&v)[N]) {
-    if (N == 1) {
-      v[0] = h2c(__ldg((const unsigned*)base + e));
-    } else if (N == 2) {
-      const uint2 a = __ldg((const uint2*)base + (e >> 1));
-      v[0] = h2c(a.x);
-      v[1] = h2c(a.y);
-    } else {
-#pragma unroll
-      for (int k = 0; k < N / 4; ++k) {
-        const uint4 a = __ldg((const uint4*)base + (e >> 2) + k);
-        v[4 * k] = h2c(a.x);
-        v[4 * k + 1] = h2c(a.y);
-        v[4 * k + 2] = h2c(a.z);
-        v[4 * k + 3] = h2c(a.w);
-      }
-    }
-  }
-  static __device__ __forceinline__ void store_raw(void* base, int64_t e, const unsigned (&w)[N]) {
-    if (N == 1) {
-      ((unsigned*)base)[e] = w[0];
-    } else if (N == 2) {
-      ((uint2*)base)[e >> 1] = make_uint2(w[0], w[1]);
-    } else {
-#pragma unroll
-      for (int k = 0; k < N / 4; ++k)
-        ((uint4*)base)[(e >> 2) + k] = make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
-    }
-  }
-};
-
 template <int N>
 __device__ __forceinline__ void load_norms(const float* nrm, int64_t e, float (&v)[N]) {
-  if (N == 1) {
+  if constexpr (N == 1) {
     v[0] = __ldg(nrm + e);
-  } else if (N == 2) {
+  } else if constexpr (N == 2) {
     const float2 a = __ldg((const float2*)nrm + (e >> 1));
     v[0] = a.x;
     v[1] = a.y;
@@ -141,9 +54,9 @@ __device__ __forceinline__ void load_norms(const float* nrm, int64_t e, float (&
 }
 template <int N>
 __device__ __forceinline__ void store_norms(float* nrm, int64_t e, const float (&v)[N]) {
-  if (N == 1) {
+  if constexpr (N == 1) {
     nrm[e] = v[0];
-  } else if (N == 2) {
+  } else if constexpr (N == 2) {
     ((float2*)nrm)[e >> 1] = make_float2(v[0], v[1]);
   } else {
 #pragma unroll
@@ -151,35 +64,18 @@ __device__ __forceinline__ void store_norms(float* nrm, int64_t e, const float (
   }
 }
 
-// Link loads: full 3x3 (F64/F32) or two rows with the third rebuilt as conj(r0 x r1).
-template <int GP>
-struct LinkIO;
-
-template <>
-struct LinkIO<GBDW_F32> {
-  static __device__ __forceinline__ void load(const void* U, size_t link, cpx<float> (&u)[3][3]) {
-    const float2* p = (const float2*)U + link * 9;
-#pragma unroll
-    for (int k = 0; k < 9; ++k) {
-      const float2 a = __ldg(p + k);
-      u[k / 3][k % 3] = {a.x, a.y};
-    }
-  }
-};
-template <>
-struct LinkIO<GBDW_F64> {
-  static __device__ __forceinline__ void load(const void* U, size_t link, cpx<double> (&u)[3][3]) {
-    const double2* p = (const double2*)U + link * 9;
-#pragma unroll
-    for (int k = 0; k < 9; ++k) {
-      const double2 a = __ldg(p + k);
-      u[k / 3][k % 3] = {a.x, a.y};
-    }
-  }
-};
-
+// ------------------------------------------------------------------ links
+// Full 3x3 (F64/F32) or two rows with the third rebuilt as conj(r0 x r1) (exact for SU(3)).
+__device__ __forceinline__ cpx<float> h2c(unsigned w) {
+  const float2 f = h2f(w);
+  return {f.x, f.y};
+}
+__device__ __forceinline__ cpx<float> b2c(unsigned w) {
+  __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162*>(&w);
+  const float2 f = __bfloat1622float2(h);
+  return {f.x, f.y};
+}
 __device__ __forceinline__ void third_row(cpx<float> (&u)[3][3]) {
-  // r2 = conj(r0 x r1)
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     const int c1 = (c + 1) % 3, c2 = (c + 2) % 3;
@@ -191,32 +87,58 @@ __device__ __forceinline__ void third_row(cpx<float> (&u)[3][3]) {
   }
 }
 
+template <int GP>
+struct LinkIO;
+template <>
+struct LinkIO<GBDW_F32> {
+  static constexpr unsigned bytes = 72;
+  template <bool SMEM = false>
+  static __device__ __forceinline__ void load(const void* U, size_t link, cpx<float> (&u)[3][3]) {
+    const float2* p = (const float2*)U + link * 9;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      const float2 a = ldv<SMEM>(p + k);
+      u[k / 3][k % 3] = {a.x, a.y};
+    }
+  }
+};
+template <>
+struct LinkIO<GBDW_F64> {
+  static constexpr unsigned bytes = 144;
+  template <bool SMEM = false>
+  static __device__ __forceinline__ void load(const void* U, size_t link, cpx<double> (&u)[3][3]) {
+    const double2* p = (const double2*)U + link * 9;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      const double2 a = ldv<SMEM>(p + k);
+      u[k / 3][k % 3] = {a.x, a.y};
+    }
+  }
+};
 template <>
 struct LinkIO<GBDW_F16> {
+  static constexpr unsigned bytes = 24;
+  template <bool SMEM = false>
   static __device__ __forceinline__ void load(const void* U, size_t link, cpx<float> (&u)[3][3]) {
     const uint2* p = (const uint2*)U + link * 3;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const uint2 a = __ldg(p + k);
+      const uint2 a = ldv<SMEM>(p + k);
       u[(2 * k) / 3][(2 * k) % 3] = h2c(a.x);
       u[(2 * k + 1) / 3][(2 * k + 1) % 3] = h2c(a.y);
     }
     third_row(u);
   }
 };
-
-__device__ __forceinline__ cpx<float> b2c(unsigned w) {
-  __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162*>(&w);
-  const float2 f = __bfloat1622float2(h);
-  return {f.x, f.y};
-}
 template <>
 struct LinkIO<GBDW_BF16> {
+  static constexpr unsigned bytes = 24;
+  template <bool SMEM = false>
   static __device__ __forceinline__ void load(const void* U, size_t link, cpx<float> (&u)[3][3]) {
     const uint2* p = (const uint2*)U + link * 3;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const uint2 a = __ldg(p + k);
+      const uint2 a = ldv<SMEM>(p + k);
       u[(2 * k) / 3][(2 * k) % 3] = b2c(a.x);
       u[(2 * k + 1) / 3][(2 * k + 1) % 3] = b2c(a.y);
     }
@@ -237,21 +159,91 @@ struct LegSpin {
   static constexpr int C1 = LT < 4 ? c1p : (c1p ^ 1);
 };
 
-// One leg for N slices: neighbour entries start at element eb (component stride LsE),
-// F16 norms at nidx.
-template <int PIN, int GP, int DAG, int N, int L, class T>
-__device__ __forceinline__ void hop_leg(const void* __restrict__ U, size_t link, const void* __restrict__ in,
-                                        const float* __restrict__ in_norm, int64_t eb, int64_t nidx,
-                                        int LsE, cpx<T> (&acc)[N][12]) {
+// ------------------------------------------------------------------ packed pair arithmetic
+__device__ __forceinline__ float2 bc(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ cp2 cadd2(cp2 a, cp2 b) { return {__fadd2_rn(a.r, b.r), __fadd2_rn(a.i, b.i)}; }
+template <int C>
+__device__ __forceinline__ cp2 cunit2(cp2 a) {
+  if constexpr (C == 0) return a;
+  else if constexpr (C == 1) return {neg2(a.r), neg2(a.i)};
+  else if constexpr (C == 2) return {neg2(a.i), a.r};
+  else return {a.i, neg2(a.r)};
+}
+// Row r of the link (one complex per colour, the same for both slices) times h.
+__device__ __forceinline__ cp2 su3_row2(const cpx<float> (&u)[3], const cp2 (&h)[3]) {
+  cp2 o;
+  o.r = __fmul2_rn(bc(u[0].r), h[0].r);
+  o.i = __fmul2_rn(bc(u[0].r), h[0].i);
+  o.r = __ffma2_rn(bc(-u[0].i), h[0].i, o.r);
+  o.i = __ffma2_rn(bc(u[0].i), h[0].r, o.i);
+#pragma unroll
+  for (int c = 1; c < 3; ++c) {
+    o.r = __ffma2_rn(bc(u[c].r), h[c].r, o.r);
+    o.i = __ffma2_rn(bc(u[c].r), h[c].i, o.i);
+    o.r = __ffma2_rn(bc(-u[c].i), h[c].i, o.r);
+    o.i = __ffma2_rn(bc(u[c].i), h[c].r, o.i);
+  }
+  return o;
+}
+
+// One leg on NP slice pairs: the neighbour's rows start at row0 of `in` (global or smem);
+// nrm points at the F16 norms of its first slice.
+template <int PIN, int DAG, int NP, int L, bool SMEM>
+__device__ __forceinline__ void hop_leg_pairs(const cpx<float> (&u)[3][3], const void* in, int64_t row0, int e0,
+                                              int LsP, const float* nrm, cp2 (&acc)[NP][12]) {
+  using S = LegSpin<DAG ? (L ^ 4) : L>;
+  cp2 h0[NP][3], h1[NP][3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    cp2 x[NP], y[NP], z[NP], w[NP];
+    Vec<PIN, 2 * NP, SMEM>::load_pairs(in, row0 + 0 * 3 + c, e0, LsP, x);
+    Vec<PIN, 2 * NP, SMEM>::load_pairs(in, row0 + S::A * 3 + c, e0, LsP, y);
+    Vec<PIN, 2 * NP, SMEM>::load_pairs(in, row0 + 1 * 3 + c, e0, LsP, z);
+    Vec<PIN, 2 * NP, SMEM>::load_pairs(in, row0 + S::B * 3 + c, e0, LsP, w);
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+      h0[q][c] = cadd2(x[q], cunit2<S::C0>(y[q]));
+      h1[q][c] = cadd2(z[q], cunit2<S::C1>(w[q]));
+    }
+  }
+  if constexpr (PIN == GBDW_F16) {
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+      const float2 nr = ldv<SMEM>(reinterpret_cast<const float2*>(nrm) + q);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        h0[q][c] = {__fmul2_rn(h0[q][c].r, nr), __fmul2_rn(h0[q][c].i, nr)};
+        h1[q][c] = {__fmul2_rn(h1[q][c].r, nr), __fmul2_rn(h1[q][c].i, nr)};
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NP; ++q)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      const cp2 u0 = su3_row2(u[r], h0[q]);
+      const cp2 u1 = su3_row2(u[r], h1[q]);
+      acc[q][0 * 3 + r] = cadd2(acc[q][0 * 3 + r], u0);
+      acc[q][1 * 3 + r] = cadd2(acc[q][1 * 3 + r], u1);
+      acc[q][S::A * 3 + r] = cadd2(acc[q][S::A * 3 + r], cunit2<conj_unit<S::C0>::v>(u0));
+      acc[q][S::B * 3 + r] = cadd2(acc[q][S::B * 3 + r], cunit2<conj_unit<S::C1>::v>(u1));
+    }
+}
+
+// One leg on N single slices (FP64, or N == 1).
+template <int PIN, int DAG, int N, int L, bool SMEM, class T>
+__device__ __forceinline__ void hop_leg_scalar(const cpx<T> (&u)[3][3], const void* in, int64_t row0, int e0, int LsP,
+                                               const float* nrm, cpx<T> (&acc)[N][12]) {
   using S = LegSpin<DAG ? (L ^ 4) : L>;
   cpx<T> h0[N][3], h1[N][3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     cpx<T> x[N], y[N], z[N], w[N];
-    SpinIO<PIN, N>::load(in, eb + int64_t(0 * 3 + c) * LsE, x);
-    SpinIO<PIN, N>::load(in, eb + int64_t(S::A * 3 + c) * LsE, y);
-    SpinIO<PIN, N>::load(in, eb + int64_t(1 * 3 + c) * LsE, z);
-    SpinIO<PIN, N>::load(in, eb + int64_t(S::B * 3 + c) * LsE, w);
+    Vec<PIN, N, SMEM>::load(in, row0 + 0 * 3 + c, e0, LsP, x);
+    Vec<PIN, N, SMEM>::load(in, row0 + S::A * 3 + c, e0, LsP, y);
+    Vec<PIN, N, SMEM>::load(in, row0 + 1 * 3 + c, e0, LsP, z);
+    Vec<PIN, N, SMEM>::load(in, row0 + S::B * 3 + c, e0, LsP, w);
 #pragma unroll
     for (int j = 0; j < N; ++j) {
       const cpx<T> ya = cunit<S::C0>(y[j]);
@@ -261,20 +253,18 @@ __device__ __forceinline__ void hop_leg(const void* __restrict__ U, size_t link,
     }
   }
   if constexpr (PIN == GBDW_F16) {
-    float nr[N];
-    load_norms<N>(in_norm, nidx, nr);
 #pragma unroll
-    for (int j = 0; j < N; ++j)
+    for (int j = 0; j < N; ++j) {
+      const float nr = ldv<SMEM>(nrm + j);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        h0[j][c].r *= nr[j];
-        h0[j][c].i *= nr[j];
-        h1[j][c].r *= nr[j];
-        h1[j][c].i *= nr[j];
+        h0[j][c].r *= nr;
+        h0[j][c].i *= nr;
+        h1[j][c].r *= nr;
+        h1[j][c].i *= nr;
       }
+    }
   }
-  cpx<T> u[3][3];
-  LinkIO<GP>::load(U, link, u);
 #pragma unroll
   for (int j = 0; j < N; ++j) {
 #pragma unroll
@@ -299,6 +289,52 @@ __device__ __forceinline__ void hop_leg(const void* __restrict__ U, size_t link,
   }
 }
 
+// Accumulator of one thread: slice pairs for FP32/FP16 with even N, single slices otherwise.
+template <int PIN, int N>
+struct Acc {
+  static constexpr bool paired = PIN != GBDW_F64 && N % 2 == 0;
+  using T = typename Arith<PIN>::T;
+  using Pair = cp2[N / 2 > 0 ? N / 2 : 1][12];
+  using Single = cpx<T>[N][12];
+  typename std::conditional<paired, Pair, Single>::type v;
+  __device__ __forceinline__ void zero() {
+    if constexpr (paired) {
+#pragma unroll
+      for (int q = 0; q < N / 2; ++q)
+#pragma unroll
+        for (int k = 0; k < 12; ++k) v[q][k] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+    } else {
+#pragma unroll
+      for (int j = 0; j < N; ++j)
+#pragma unroll
+        for (int k = 0; k < 12; ++k) v[j][k] = {T(0), T(0)};
+    }
+  }
+  __device__ __forceinline__ void unpack(cpx<T> (&a)[N][12]) const {
+    if constexpr (paired) {
+#pragma unroll
+      for (int q = 0; q < N / 2; ++q)
+#pragma unroll
+        for (int k = 0; k < 12; ++k) {
+          a[2 * q][k] = {v[q][k].r.x, v[q][k].i.x};
+          a[2 * q + 1][k] = {v[q][k].r.y, v[q][k].i.y};
+        }
+    } else {
+#pragma unroll
+      for (int j = 0; j < N; ++j)
+#pragma unroll
+        for (int k = 0; k < 12; ++k) a[j][k] = v[j][k];
+    }
+  }
+};
+
+template <int PIN, int DAG, int N, int L, bool SMEM>
+__device__ __forceinline__ void hop_leg(const cpx<typename Arith<PIN>::T> (&u)[3][3], const void* in, int64_t row0,
+                                        int e0, int LsP, const float* nrm, Acc<PIN, N>& acc) {
+  if constexpr (Acc<PIN, N>::paired) hop_leg_pairs<PIN, DAG, N / 2, L, SMEM>(u, in, row0, e0, LsP, nrm, acc.v);
+  else hop_leg_scalar<PIN, DAG, N, L, SMEM>(u, in, row0, e0, LsP, nrm, acc.v);
+}
+
 // ------------------------------------------------------------------ kernel parameters
 struct DhopParams {
   const void* U;
@@ -309,7 +345,8 @@ struct DhopParams {
   const uint32_t* nbr4;  // fast path
   const uint32_t* nbr5;  // general path
   int64_t nsite;
-  int LsE;               // innermost extent (Ls * nrhs)
+  int LsE;               // slices per row (Ls * nrhs)
+  int LsP;               // stored slots per row (LsE rounded up to even for F32/F16)
   int Ls;
   double a5;             // 5 - M5   (M epilogue)
   double mf;             // domain-wall mass (M epilogue)
@@ -319,12 +356,13 @@ struct DhopParams {
   unsigned* err;         // device error word (bounded waits that expired)
 };
 
-// Writes N slices of result spinor v[N][12] at element eo (and norms at no for F16);
-// returns the sum of squares of what was stored (as read back in arithmetic precision).
+// Writes N slices of v[N][12] (slices e0.., norms for F16); returns the sum of squares of
+// what was stored.
 template <int POUT, int N, class T>
-__device__ __forceinline__ float store_spinor(void* out, float* out_norm, int64_t eo, int64_t no, int LsE,
+__device__ __forceinline__ float store_spinor(void* out, float* out_norm, int64_t site, int e0, int LsE, int LsP,
                                               const cpx<T> (&v)[N][12]) {
   float nrm2 = 0.f;
+  const int64_t row0 = site * 12;
   if constexpr (POUT == GBDW_F16) {
     float scale[N], nm[N];
 #pragma unroll
@@ -335,18 +373,19 @@ __device__ __forceinline__ float store_spinor(void* out, float* out_norm, int64_
       nm[j] = m;
       scale[j] = m > 0.f ? 1.0f / m : 0.f;
     }
-    store_norms<N>(out_norm, no, nm);
+    store_norms<N>(out_norm, site * LsE + e0, nm);
 #pragma unroll
     for (int k = 0; k < 12; ++k) {
-      unsigned w[N];
+      cpx<float> w[N];
 #pragma unroll
       for (int j = 0; j < N; ++j) {
-        w[j] = c2h(float(v[j][k].r) * scale[j], float(v[j][k].i) * scale[j]);
-        const cpx<float> b = h2c(w[j]);
-        nrm2 = fmaf(b.r * nm[j], b.r * nm[j], nrm2);
-        nrm2 = fmaf(b.i * nm[j], b.i * nm[j], nrm2);
+        w[j] = {float(v[j][k].r) * scale[j], float(v[j][k].i) * scale[j]};
+        // norm of the value as stored
+        const float2 b = __half22float2(__floats2half2_rn(w[j].r, w[j].i));
+        nrm2 = fmaf(b.x * nm[j], b.x * nm[j], nrm2);
+        nrm2 = fmaf(b.y * nm[j], b.y * nm[j], nrm2);
       }
-      SpinIO<GBDW_F16, N>::store_raw(out, eo + int64_t(k) * LsE, w);
+      Vec<GBDW_F16, N>::store_scaled(out, row0 + k, e0, LsP, w);
     }
   } else {
     using TO = typename Arith<POUT>::T;
@@ -359,13 +398,12 @@ __device__ __forceinline__ float store_spinor(void* out, float* out_norm, int64_
         nrm2 = fmaf(float(w[j].r), float(w[j].r), nrm2);
         nrm2 = fmaf(float(w[j].i), float(w[j].i), nrm2);
       }
-      SpinIO<POUT, N>::store(out, eo + int64_t(k) * LsE, w);
+      Vec<POUT, N>::store(out, row0 + k, e0, LsP, w);
     }
   }
   return nrm2;
 }
 
-// Double-precision sum of squares for FP64 outputs (exact accumulation of the stored values).
 template <int N>
 __device__ __forceinline__ double sumsq(const cpx<double> (&v)[N][12]) {
   double s = 0.0;
@@ -376,7 +414,7 @@ __device__ __forceinline__ double sumsq(const cpx<double> (&v)[N][12]) {
   return s;
 }
 template <int N>
-__device__ __forceinline__ double sumsq(const cpx<float> (&v)[N][12]) {
+__device__ __forceinline__ double sumsq(const cpx<float> (&)[N][12]) {
   return 0.0;
 }
 
@@ -388,12 +426,13 @@ __device__ __forceinline__ double sumsq(const cpx<float> (&v)[N][12]) {
 template <int PIN, int DAG, int N, class T>
 __device__ __forceinline__ void dwf_epilogue(const DhopParams& p, int64_t site, int s0, cpx<T> (&acc)[N][12]) {
   const int Ls = p.Ls;
-  const int64_t base = site * 12 * int64_t(Ls);
+  const int LsP = p.LsP;
+  const int64_t row0 = site * 12;
   cpx<T> cen[N][12];
 #pragma unroll
   for (int k = 0; k < 12; ++k) {
     cpx<T> x[N];
-    SpinIO<PIN, N>::load(p.in, base + int64_t(k) * Ls + s0, x);
+    Vec<PIN, N>::load(p.in, row0 + k, s0, LsP, x);
 #pragma unroll
     for (int j = 0; j < N; ++j) cen[j][k] = x[j];
   }
@@ -401,17 +440,13 @@ __device__ __forceinline__ void dwf_epilogue(const DhopParams& p, int64_t site, 
   const int shi = (s0 + N == Ls) ? 0 : s0 + N;
   const T flo = (s0 == 0) ? T(-p.mf) : T(1);
   const T fhi = (s0 + N == Ls) ? T(-p.mf) : T(1);
-  // spins taken from s-1 and from s+1
   constexpr int LO0 = DAG ? 2 : 0;  // first spin fed by psi(s-1)
   constexpr int HI0 = DAG ? 0 : 2;  // first spin fed by psi(s+1)
   cpx<T> lo[6], hi[6];
 #pragma unroll
   for (int k = 0; k < 6; ++k) {
-    cpx<T> x[1], y[1];
-    SpinIO<PIN, 1>::load(p.in, base + int64_t(LO0 * 3 + k) * Ls + slo, x);
-    SpinIO<PIN, 1>::load(p.in, base + int64_t(HI0 * 3 + k) * Ls + shi, y);
-    lo[k] = x[0];
-    hi[k] = y[0];
+    lo[k] = Elem<PIN>::ld(p.in, row0 + LO0 * 3 + k, slo, LsP);
+    hi[k] = Elem<PIN>::ld(p.in, row0 + HI0 * 3 + k, shi, LsP);
   }
   T nlo = flo, nhi = fhi;
   if constexpr (PIN == GBDW_F16) {
@@ -437,7 +472,6 @@ __device__ __forceinline__ void dwf_epilogue(const DhopParams& p, int64_t site, 
     }
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
-      // psi(s-1) feeds spins LO0, LO0+1
       const cpx<T> m = (j == 0) ? cpx<T>{lo[k].r * nlo, lo[k].i * nlo} : cen[j - 1 < 0 ? 0 : j - 1][LO0 * 3 + k];
       acc[j][LO0 * 3 + k].r -= m.r;
       acc[j][LO0 * 3 + k].i -= m.i;
@@ -450,22 +484,23 @@ __device__ __forceinline__ void dwf_epilogue(const DhopParams& p, int64_t site, 
 
 // ------------------------------------------------------------------ kernels
 // Hopping sum for one thread: site and first slice s0 of N consecutive slices.
-template <int PIN, int GP, int DAG, int N, class T>
-__device__ __forceinline__ void dhop_thread(const DhopParams& p, unsigned site, int s0, cpx<T> (&acc)[N][12]) {
-#pragma unroll
-  for (int j = 0; j < N; ++j)
-#pragma unroll
-    for (int k = 0; k < 12; ++k) acc[j][k] = {T(0), T(0)};
+template <int PIN, int GP, int DAG, int N>
+__device__ __forceinline__ void dhop_thread(const DhopParams& p, unsigned site, int s0,
+                                            cpx<typename Arith<PIN>::T> (&out)[N][12]) {
+  using T = typename Arith<PIN>::T;
+  Acc<PIN, N> acc;
+  acc.zero();
   const uint32_t* nb = p.nbr4 + size_t(site) * 8;
-  const int64_t LsE = p.LsE;
 #define GBDW_LEG(L)                                                                                  \
   {                                                                                                  \
     const int64_t n = __ldg(nb + L);                                                                 \
-    hop_leg<PIN, GP, DAG, N, L>(p.U, size_t(site) * 8 + L, p.in, p.in_norm, n * 12 * LsE + s0,       \
-                                n * LsE + s0, p.LsE, acc);                                           \
+    cpx<T> u[3][3];                                                                                  \
+    LinkIO<GP>::load(p.U, size_t(site) * 8 + L, u);                                                  \
+    hop_leg<PIN, DAG, N, L, false>(u, p.in, n * 12, s0, p.LsP, p.in_norm + n * p.LsE + s0, acc);     \
   }
   GBDW_LEG(0) GBDW_LEG(1) GBDW_LEG(2) GBDW_LEG(3) GBDW_LEG(4) GBDW_LEG(5) GBDW_LEG(6) GBDW_LEG(7)
 #undef GBDW_LEG
+  acc.unpack(out);
 }
 
 // EPI 0: out = Dhop(in) ; EPI 1: out = M(in) (Shamir).  |out|^2 fused when p.partials != 0.
@@ -483,9 +518,8 @@ __global__ void __launch_bounds__(256) k_dhop(const DhopParams p) {
     cpx<T> acc[N][12];
     dhop_thread<PIN, GP, DAG, N>(p, site, s0, acc);
     if constexpr (EPI == 1) dwf_epilogue<PIN, DAG, N>(p, site, s0, acc);
-    part = store_spinor<POUT, N>(p.out, p.out_norm, int64_t(site) * 12 * p.LsE + s0, int64_t(site) * p.LsE + s0,
-                                 p.LsE, acc);
-    if (POUT == GBDW_F64) dpart = sumsq<N>(acc);
+    part = store_spinor<POUT, N>(p.out, p.out_norm, site, s0, p.LsE, p.LsP, acc);
+    if constexpr (POUT == GBDW_F64) dpart = sumsq<N>(acc);
   }
   if (p.partials) {
     double v[1] = {POUT == GBDW_F64 ? dpart : double(part)};
@@ -501,28 +535,32 @@ __global__ void __launch_bounds__(256) k_dhop_general(const DhopParams p) {
   if (tid >= unsigned(p.nsite) * unsigned(p.Ls)) return;
   const unsigned site = tid / unsigned(p.Ls);
   const int s = int(tid - site * unsigned(p.Ls));
-  cpx<T> acc[1][12];
-#pragma unroll
-  for (int k = 0; k < 12; ++k) acc[0][k] = {T(0), T(0)};
+  Acc<PIN, 1> acc;
+  acc.zero();
   const uint32_t* nb = p.nbr5 + size_t(tid) * 8;
   const int64_t Ls = p.Ls;
-#define GBDW_LEG(L)                                                                                   \
-  {                                                                                                   \
-    const int64_t n5 = __ldg(nb + L);                                                                 \
-    const int64_t ns = n5 / Ls, sn = n5 - ns * Ls;                                                    \
-    hop_leg<PIN, GP, DAG, 1, L>(p.U, size_t(site) * 8 + L, p.in, p.in_norm, ns * 12 * Ls + sn, n5, p.Ls, acc); \
+#define GBDW_LEG(L)                                                                            \
+  {                                                                                            \
+    const int64_t n5 = __ldg(nb + L);                                                          \
+    const int64_t ns = n5 / Ls;                                                                \
+    const int sn = int(n5 - ns * Ls);                                                          \
+    cpx<T> u[3][3];                                                                            \
+    LinkIO<GP>::load(p.U, size_t(site) * 8 + L, u);                                            \
+    hop_leg<PIN, DAG, 1, L, false>(u, p.in, ns * 12, sn, p.LsP, p.in_norm + n5, acc);         \
   }
   GBDW_LEG(0) GBDW_LEG(1) GBDW_LEG(2) GBDW_LEG(3) GBDW_LEG(4) GBDW_LEG(5) GBDW_LEG(6) GBDW_LEG(7)
 #undef GBDW_LEG
-  store_spinor<PIN, 1>(p.out, p.out_norm, int64_t(site) * 12 * Ls + s, int64_t(site) * Ls + s, p.Ls, acc);
+  cpx<T> out[1][12];
+  acc.unpack(out);
+  store_spinor<PIN, 1>(p.out, p.out_norm, site, s, p.Ls, p.LsP, out);
 }
 
 // ------------------------------------------------------------------ launch dispatch
 struct DhopLaunch {
-  int threads;     // per CTA (target; the staged kernel rounds to whole sites)
+  int threads;     // per CTA (target; the staged kernels round to whole sites)
   int spt;         // slices per thread
-  int mode = 0;    // 0: direct loads, 1: TMA-staged neighbour blocks
-  int stages = 4;  // staged kernel: depth of the leg ring
+  int mode = 0;    // 0: direct loads, 1: TMA-staged (CTA ring), 2: TMA-staged (one ring per warp)
+  int stages = 4;  // staged kernels: depth of the leg ring
 };
 
 // Implemented per precision family in dhop_f64.cu / dhop_f32.cu / dhop_f16.cu.
@@ -530,7 +568,8 @@ int launch_dhop_f64(const DhopParams& p, int dag, int epi, DhopLaunch L);
 int launch_dhop_f32(const DhopParams& p, int dag, int epi, DhopLaunch L);
 int launch_dhop_f16(const DhopParams& p, int gprec, int dag, int epi, DhopLaunch L);
 int launch_dhop_general(const DhopParams& p, int prec, int dag);
-// Sites per CTA and dynamic shared memory of the staged kernel, or false if it cannot run.
+// Sites per CTA, threads and dynamic shared memory of a staged form (L.mode 1 or 2), or false
+// if that form cannot run for this precision and extent.
 bool tma_shape(int prec, int LsE, DhopLaunch L, int* NS, int* threads, size_t* smem);
 
 }  // namespace gbdw

@@ -38,12 +38,38 @@ int go_tma(const DhopParams& p, DhopLaunch L) {
   return GBDW_OK;
 }
 
-// Slice splits compiled per precision: S1 and S2 for both forms.
+template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int STAGES>
+int go_tmaw(const DhopParams& p, DhopLaunch L) {
+  int NS = 0, threads = 0;
+  size_t smem = 0;
+  if (!tma_shape(PIN, p.LsE, L, &NS, &threads, &smem)) {
+    set_error("warp-staged hopping kernel: no admissible shape for this extent");
+    return GBDW_ERR_INVALID;
+  }
+  auto kern = k_dhop_tmaw<PIN, POUT, GP, DAG, N, EPI, STAGES>;
+  static bool opted_in = false;
+  if (!opted_in) {
+    cudaFuncAttributes fa;
+    GBDW_CUDA(cudaFuncGetAttributes(&fa, kern));
+    const size_t limit = max_dynamic_smem() + 1024 - fa.sharedSizeBytes;
+    GBDW_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(limit)));
+    opted_in = true;
+  }
+  const unsigned blocks = unsigned((p.nsite + NS - 1) / NS);
+  kern<<<blocks, threads, smem, stream()>>>(p);
+  GBDW_LAUNCHED();
+  return GBDW_OK;
+}
+
+// Slice splits compiled per precision: S1 and S2 for the staged forms.
 template <int PIN, int POUT, int GP, int DAG, int EPI, int S1, int S2>
 int by_shape(const DhopParams& p, DhopLaunch L) {
   if (L.mode == 1) {
     if (L.spt == S1) return L.stages == 2 ? go_tma<PIN, POUT, GP, DAG, S1, EPI, 2>(p, L) : go_tma<PIN, POUT, GP, DAG, S1, EPI, 4>(p, L);
     if (L.spt == S2) return L.stages == 2 ? go_tma<PIN, POUT, GP, DAG, S2, EPI, 2>(p, L) : go_tma<PIN, POUT, GP, DAG, S2, EPI, 4>(p, L);
+  } else if (L.mode == 2) {
+    if (L.spt == S1) return L.stages == 2 ? go_tmaw<PIN, POUT, GP, DAG, S1, EPI, 2>(p, L) : go_tmaw<PIN, POUT, GP, DAG, S1, EPI, 4>(p, L);
+    if (L.spt == S2) return L.stages == 2 ? go_tmaw<PIN, POUT, GP, DAG, S2, EPI, 2>(p, L) : go_tmaw<PIN, POUT, GP, DAG, S2, EPI, 4>(p, L);
   } else {
     if (L.spt == 1) return go_direct<PIN, POUT, GP, DAG, 1, EPI>(p, L);
     if (L.spt == 2) return go_direct<PIN, POUT, GP, DAG, 2, EPI>(p, L);

@@ -33,12 +33,14 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
                "l"(src), "r"(bytes), "r"(smem_u32(bar))
                : "memory");
 }
+// try_wait with a suspend-time hint: a waiting thread sleeps (up to 20 us) until the phase
+// completes instead of spinning through issue slots the computing warps need.
 __device__ __forceinline__ bool mbar_try(uint64_t* bar, unsigned parity) {
   uint32_t ok;
   asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n}\n"
       : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(20000u)
       : "memory");
   return ok != 0;
 }
@@ -64,164 +66,20 @@ struct ESz {
   static constexpr unsigned v = P == GBDW_F64 ? 16 : P == GBDW_F32 ? 8 : 4;
 };
 
-// Shared-memory loads of N consecutive complex entries (no __ldg: the data is in smem).
-template <int P, int N>
-__device__ __forceinline__ void lds(const unsigned char* base, int e, cpx<typename Arith<P>::T> (&v)[N]) {
-  if constexpr (P == GBDW_F64) {
-#pragma unroll
-    for (int k = 0; k < N; ++k) {
-      const double2 a = reinterpret_cast<const double2*>(base)[e + k];
-      v[k] = {a.x, a.y};
-    }
-  } else if constexpr (P == GBDW_F32) {
-    if constexpr (N == 1) {
-      const float2 a = reinterpret_cast<const float2*>(base)[e];
-      v[0] = {a.x, a.y};
-    } else {
-#pragma unroll
-      for (int k = 0; k < N / 2; ++k) {
-        const float4 a = reinterpret_cast<const float4*>(base)[(e >> 1) + k];
-        v[2 * k] = {a.x, a.y};
-        v[2 * k + 1] = {a.z, a.w};
-      }
-    }
-  } else {
-    if constexpr (N == 1) {
-      v[0] = h2c(reinterpret_cast<const unsigned*>(base)[e]);
-    } else if constexpr (N == 2) {
-      const uint2 a = reinterpret_cast<const uint2*>(base)[e >> 1];
-      v[0] = h2c(a.x);
-      v[1] = h2c(a.y);
-    } else {
-#pragma unroll
-      for (int k = 0; k < N / 4; ++k) {
-        const uint4 a = reinterpret_cast<const uint4*>(base)[(e >> 2) + k];
-        v[4 * k] = h2c(a.x);
-        v[4 * k + 1] = h2c(a.y);
-        v[4 * k + 2] = h2c(a.z);
-        v[4 * k + 3] = h2c(a.w);
-      }
-    }
-  }
-}
-
-// A site's 8 doubled links in shared memory (staged as one block per site).
-template <int GP>
-struct LinkSmem;
-template <>
-struct LinkSmem<GBDW_F32> {
-  static constexpr unsigned bytes = 8 * 72;
-  static __device__ __forceinline__ void load(const unsigned char* site_links, int L, cpx<float> (&u)[3][3]) {
-    const float2* p = reinterpret_cast<const float2*>(site_links) + L * 9;
-#pragma unroll
-    for (int k = 0; k < 9; ++k) u[k / 3][k % 3] = {p[k].x, p[k].y};
-  }
-};
-template <>
-struct LinkSmem<GBDW_F64> {
-  static constexpr unsigned bytes = 8 * 144;
-  static __device__ __forceinline__ void load(const unsigned char* site_links, int L, cpx<double> (&u)[3][3]) {
-    const double2* p = reinterpret_cast<const double2*>(site_links) + L * 9;
-#pragma unroll
-    for (int k = 0; k < 9; ++k) u[k / 3][k % 3] = {p[k].x, p[k].y};
-  }
-};
-template <>
-struct LinkSmem<GBDW_F16> {
-  static constexpr unsigned bytes = 8 * 24;
-  static __device__ __forceinline__ void load(const unsigned char* site_links, int L, cpx<float> (&u)[3][3]) {
-    const unsigned* p = reinterpret_cast<const unsigned*>(site_links) + L * 6;
-#pragma unroll
-    for (int k = 0; k < 6; ++k) u[k / 3][k % 3] = h2c(p[k]);
-    third_row(u);
-  }
-};
-template <>
-struct LinkSmem<GBDW_BF16> {
-  static constexpr unsigned bytes = 8 * 24;
-  static __device__ __forceinline__ void load(const unsigned char* site_links, int L, cpx<float> (&u)[3][3]) {
-    const unsigned* p = reinterpret_cast<const unsigned*>(site_links) + L * 6;
-#pragma unroll
-    for (int k = 0; k < 6; ++k) u[k / 3][k % 3] = b2c(p[k]);
-    third_row(u);
-  }
-};
-
-// One leg from a staged neighbour block (blk: the 12*LsE entries, nrm: its norms for F16)
-// with the site's staged links.
-template <int PIN, int GP, int DAG, int N, int L, class T>
-__device__ __forceinline__ void hop_leg_smem(const unsigned char* site_links, const unsigned char* blk,
-                                             const float* nrm, int s0, int LsE, cpx<T> (&acc)[N][12]) {
-  using S = LegSpin<DAG ? (L ^ 4) : L>;
-  cpx<T> u[3][3];
-  LinkSmem<GP>::load(site_links, L, u);
-  cpx<T> h0[N][3], h1[N][3];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    cpx<T> x[N], y[N], z[N], w[N];
-    lds<PIN, N>(blk, (0 * 3 + c) * LsE + s0, x);
-    lds<PIN, N>(blk, (S::A * 3 + c) * LsE + s0, y);
-    lds<PIN, N>(blk, (1 * 3 + c) * LsE + s0, z);
-    lds<PIN, N>(blk, (S::B * 3 + c) * LsE + s0, w);
-#pragma unroll
-    for (int j = 0; j < N; ++j) {
-      const cpx<T> ya = cunit<S::C0>(y[j]);
-      const cpx<T> wb = cunit<S::C1>(w[j]);
-      h0[j][c] = {x[j].r + ya.r, x[j].i + ya.i};
-      h1[j][c] = {z[j].r + wb.r, z[j].i + wb.i};
-    }
-  }
-  if constexpr (PIN == GBDW_F16) {
-#pragma unroll
-    for (int j = 0; j < N; ++j) {
-      const float nr = nrm[s0 + j];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        h0[j][c].r *= nr;
-        h0[j][c].i *= nr;
-        h1[j][c].r *= nr;
-        h1[j][c].i *= nr;
-      }
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < N; ++j) {
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-      cpx<T> u0 = {T(0), T(0)}, u1 = {T(0), T(0)};
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        cmac(u0, u[r][c], h0[j][c]);
-        cmac(u1, u[r][c], h1[j][c]);
-      }
-      const cpx<T> ra = cunit<conj_unit<S::C0>::v>(u0);
-      const cpx<T> rb = cunit<conj_unit<S::C1>::v>(u1);
-      acc[j][0 * 3 + r].r += u0.r;
-      acc[j][0 * 3 + r].i += u0.i;
-      acc[j][1 * 3 + r].r += u1.r;
-      acc[j][1 * 3 + r].i += u1.i;
-      acc[j][S::A * 3 + r].r += ra.r;
-      acc[j][S::A * 3 + r].i += ra.i;
-      acc[j][S::B * 3 + r].r += rb.r;
-      acc[j][S::B * 3 + r].i += rb.i;
-    }
-  }
-}
-
-
 // Shared memory: STAGES rings of NS neighbour blocks (+ norms), then the NS sites' links,
 // then STAGES+1 mbarriers (the last one for the links).
 template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int STAGES>
 __global__ void __launch_bounds__(256) k_dhop_tma(const DhopParams p, int NS) {
   using T = typename Arith<PIN>::T;
   extern __shared__ __align__(128) unsigned char smem[];
-  const int LsE = p.LsE;
+  const int LsE = p.LsE, LsP = p.LsP;
   const int Tps = LsE / N;
-  const unsigned blk = 12u * unsigned(LsE) * ESz<PIN>::v;
+  const unsigned blk = 12u * unsigned(LsP) * ESz<PIN>::v;
   const unsigned nblk = (PIN == GBDW_F16) ? 4u * unsigned(LsE) : 0u;
   const unsigned stage = unsigned(NS) * (blk + nblk);
+  constexpr unsigned LB = 8 * LinkIO<GP>::bytes;  // a site's 8 links
   unsigned char* links = smem + STAGES * stage;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(links + NS * LinkSmem<GP>::bytes);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(links + NS * LB);
   const int tid = threadIdx.x;
   const int64_t site0 = int64_t(blockIdx.x) * NS;
   const int nvalid = int(min(int64_t(NS), p.nsite - site0));
@@ -258,23 +116,18 @@ __global__ void __launch_bounds__(256) k_dhop_tma(const DhopParams p, int NS) {
 
   // links of the CTA's sites: one block of 8 links per site
   if (tid < nvalid)
-    bulk_g2s(links + tid * LinkSmem<GP>::bytes,
-             (const unsigned char*)p.U + (site0 + tid) * int64_t(LinkSmem<GP>::bytes), LinkSmem<GP>::bytes,
-             &bars[STAGES]);
-  if (tid == 0) mbar_arrive_expect_tx(&bars[STAGES], unsigned(nvalid) * LinkSmem<GP>::bytes);
+    bulk_g2s(links + tid * LB, (const unsigned char*)p.U + (site0 + tid) * int64_t(LB), LB, &bars[STAGES]);
+  if (tid == 0) mbar_arrive_expect_tx(&bars[STAGES], unsigned(nvalid) * LB);
 
 #pragma unroll
   for (int L = 0; L < STAGES && L < 8; ++L) issue(L, L);
 
-  cpx<T> acc[N][12];
-#pragma unroll
-  for (int j = 0; j < N; ++j)
-#pragma unroll
-    for (int k = 0; k < 12; ++k) acc[j][k] = {T(0), T(0)};
+  Acc<PIN, N> acc;
+  acc.zero();
 
   int consumed = 0;  // legs whose stage has been waited for
   bool failed = __syncthreads_or(!mbar_wait_bounded(&bars[STAGES], 0, kWaitLimitNs));
-  const unsigned char* my_links = links + (active ? sl : 0) * LinkSmem<GP>::bytes;
+  const unsigned char* my_links = links + (active ? sl : 0) * LB;
 #define GBDW_TMA_LEG(L)                                                                                     \
   if (!failed) {                                                                                            \
     const int st = (L) % STAGES;                                                                            \
@@ -283,10 +136,12 @@ __global__ void __launch_bounds__(256) k_dhop_tma(const DhopParams p, int NS) {
     if (!failed) {                                                                                          \
       consumed = (L) + 1;                                                                                   \
       const unsigned char* base = smem + st * stage;                                                        \
-      if (active)                                                                                           \
-        hop_leg_smem<PIN, GP, DAG, N, L>(my_links, base + sl * blk,                                          \
-                                         reinterpret_cast<const float*>(base + NS * blk + sl * nblk), s0,   \
-                                         LsE, acc);                                                         \
+      if (active) {                                                                                         \
+        cpx<T> u[3][3];                                                                                     \
+        LinkIO<GP>::template load<true>(my_links, (L), u);                                                  \
+        hop_leg<PIN, DAG, N, L, true>(u, base + sl * blk, 0, s0, LsP,                                       \
+                                      reinterpret_cast<const float*>(base + NS * blk + sl * nblk) + s0, acc); \
+      }                                                                                                     \
       if ((L) + STAGES < 8) {                                                                               \
         __syncthreads();                                                                                    \
         fence_proxy_async_smem();                                                                           \
@@ -308,12 +163,135 @@ __global__ void __launch_bounds__(256) k_dhop_tma(const DhopParams p, int NS) {
   double dpart = 0.0;
   if (active && !failed) {
     const int64_t site = site0 + sl;
-    if constexpr (EPI == 1) dwf_epilogue<PIN, DAG, N>(p, site, s0, acc);
-    part = store_spinor<POUT, N>(p.out, p.out_norm, site * 12 * LsE + s0, site * LsE + s0, LsE, acc);
-    if constexpr (POUT == GBDW_F64) dpart = sumsq<N>(acc);
+    cpx<T> out[N][12];
+    acc.unpack(out);
+    if constexpr (EPI == 1) dwf_epilogue<PIN, DAG, N>(p, site, s0, out);
+    part = store_spinor<POUT, N>(p.out, p.out_norm, site, s0, LsE, LsP, out);
+    if constexpr (POUT == GBDW_F64) dpart = sumsq<N>(out);
   }
   if (p.partials) {
     // also reached after a timeout, so the grid reduction stays consistent
+    double v[1] = {POUT == GBDW_F64 ? dpart : double(part)};
+    grid_sum<1>(v, p.partials, p.counter, p.result);
+  }
+}
+
+// ------------------------------------------------------------------ warp-autonomous staged kernel
+// Same staging as k_dhop_tma, but every warp runs its own ring: a warp owns NSW = 32/Tps
+// sites (Tps = LsE/N threads per site, at most 32), its own STAGES buffers, its own links
+// block and its own mbarriers, and synchronises only with __syncwarp.  No CTA-wide barrier
+// sits between the legs, so a warp that finished its leg refills its buffer at once.
+// Shared memory per warp: STAGES*NSW*(blk+nblk) + NSW*links + (STAGES+1)*8 bytes.
+template <int PIN, int GP>
+__host__ __device__ inline unsigned tmaw_warp_bytes(int NSW, int LsE, int LsP, int STAGES) {
+  const unsigned esz = PIN == GBDW_F64 ? 16u : PIN == GBDW_F32 ? 8u : 4u;
+  const unsigned blk = 12u * unsigned(LsP) * esz + (PIN == GBDW_F16 ? 4u * unsigned(LsE) : 0u);
+  const unsigned lb = GP == GBDW_F64 ? 8u * 144u : GP == GBDW_F32 ? 8u * 72u : 8u * 24u;
+  // barrier area padded to 16 bytes so every warp's buffers stay 16-byte aligned for TMA
+  return unsigned(STAGES) * unsigned(NSW) * blk + unsigned(NSW) * lb + ((unsigned(STAGES + 1) * 8u + 15u) & ~15u);
+}
+
+template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int STAGES>
+__global__ void __launch_bounds__(256) k_dhop_tmaw(const DhopParams p) {
+  using T = typename Arith<PIN>::T;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int LsE = p.LsE, LsP = p.LsP;
+  const int Tps = LsE / N;
+  const int NSW = 32 / Tps;
+  const unsigned blk = 12u * unsigned(LsP) * ESz<PIN>::v;
+  const unsigned nblk = (PIN == GBDW_F16) ? 4u * unsigned(LsE) : 0u;
+  const unsigned stage = unsigned(NSW) * (blk + nblk);
+  constexpr unsigned LB = 8 * LinkIO<GP>::bytes;  // a site's 8 links
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned char* wbase = smem + warp * tmaw_warp_bytes<PIN, GP>(NSW, LsE, LsP, STAGES);
+  unsigned char* links = wbase + STAGES * stage;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(links + NSW * LB);
+  const int64_t site0 = (int64_t(blockIdx.x) * (blockDim.x >> 5) + warp) * NSW;
+  const int nvalid = int(max(int64_t(0), min(int64_t(NSW), p.nsite - site0)));
+  const int sl = lane / Tps;
+  const int s0 = (lane - sl * Tps) * N;
+  const bool active = sl < nvalid;
+  const unsigned expect = unsigned(nvalid) * (blk + nblk);
+
+  Acc<PIN, N> acc;
+  acc.zero();
+  bool failed = false;
+  int consumed = 0;
+
+  if (nvalid > 0) {
+    if (lane == 0) {
+#pragma unroll
+      for (int s = 0; s <= STAGES; ++s) mbar_init(&bars[s], 1);
+      fence_mbar_init();
+    }
+    uint32_t nb[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (lane < nvalid) {
+      const uint4* q = reinterpret_cast<const uint4*>(p.nbr4 + (site0 + lane) * 8);
+      const uint4 a = __ldg(q), b = __ldg(q + 1);
+      nb[0] = a.x; nb[1] = a.y; nb[2] = a.z; nb[3] = a.w;
+      nb[4] = b.x; nb[5] = b.y; nb[6] = b.z; nb[7] = b.w;
+    }
+    __syncwarp();
+    auto issue = [&](int L, int st) {
+      unsigned char* base = wbase + st * stage;
+      if (lane < nvalid) {
+        const int64_t n = nb[L];
+        bulk_g2s(base + lane * blk, (const unsigned char*)p.in + n * blk, blk, &bars[st]);
+        if constexpr (PIN == GBDW_F16)
+          bulk_g2s(base + NSW * blk + lane * nblk, (const unsigned char*)p.in_norm + n * nblk, nblk, &bars[st]);
+      }
+      if (lane == 0) mbar_arrive_expect_tx(&bars[st], expect);
+    };
+    if (lane < nvalid)
+      bulk_g2s(links + lane * LB, (const unsigned char*)p.U + (site0 + lane) * int64_t(LB), LB, &bars[STAGES]);
+    if (lane == 0) mbar_arrive_expect_tx(&bars[STAGES], unsigned(nvalid) * LB);
+#pragma unroll
+    for (int L = 0; L < STAGES && L < 8; ++L) issue(L, L);
+
+    failed = __any_sync(0xffffffffu, !mbar_wait_bounded(&bars[STAGES], 0, kWaitLimitNs));
+    const unsigned char* my_links = links + (active ? sl : 0) * LB;
+#define GBDW_TMAW_LEG(L)                                                                                   \
+  if (!failed) {                                                                                           \
+    const int st = (L) % STAGES;                                                                           \
+    failed = __any_sync(0xffffffffu, !mbar_wait_bounded(&bars[st], ((L) / STAGES) & 1, kWaitLimitNs));    \
+    if (!failed) {                                                                                         \
+      consumed = (L) + 1;                                                                                  \
+      const unsigned char* base = wbase + st * stage;                                                      \
+      if (active) {                                                                                        \
+        cpx<T> u[3][3];                                                                                    \
+        LinkIO<GP>::template load<true>(my_links, (L), u);                                                 \
+        hop_leg<PIN, DAG, N, L, true>(u, base + sl * blk, 0, s0, LsP,                                      \
+                                      reinterpret_cast<const float*>(base + NSW * blk + sl * nblk) + s0, acc); \
+      }                                                                                                    \
+      if ((L) + STAGES < 8) {                                                                              \
+        __syncwarp();                                                                                      \
+        fence_proxy_async_smem();                                                                          \
+        issue((L) + STAGES, st);                                                                           \
+      }                                                                                                    \
+    }                                                                                                      \
+  }
+    GBDW_TMAW_LEG(0) GBDW_TMAW_LEG(1) GBDW_TMAW_LEG(2) GBDW_TMAW_LEG(3)
+    GBDW_TMAW_LEG(4) GBDW_TMAW_LEG(5) GBDW_TMAW_LEG(6) GBDW_TMAW_LEG(7)
+#undef GBDW_TMAW_LEG
+    if (failed && lane == 0) {
+      atomicOr(p.err, unsigned(GBDW_ERR_TIMEOUT));
+      const int issued = min(8, consumed + STAGES);
+      for (int L = consumed; L < issued; ++L) mbar_wait_bounded(&bars[L % STAGES], (L / STAGES) & 1, kWaitLimitNs);
+      mbar_wait_bounded(&bars[STAGES], 0, kWaitLimitNs);
+    }
+    __syncwarp();
+  }
+  float part = 0.f;
+  double dpart = 0.0;
+  if (active && !failed) {
+    const int64_t site = site0 + sl;
+    cpx<T> out[N][12];
+    acc.unpack(out);
+    if constexpr (EPI == 1) dwf_epilogue<PIN, DAG, N>(p, site, s0, out);
+    part = store_spinor<POUT, N>(p.out, p.out_norm, site, s0, LsE, LsP, out);
+    if constexpr (POUT == GBDW_F64) dpart = sumsq<N>(out);
+  }
+  if (p.partials) {
     double v[1] = {POUT == GBDW_F64 ? dpart : double(part)};
     grid_sum<1>(v, p.partials, p.counter, p.result);
   }

@@ -6,6 +6,7 @@
 
 #include "common.cuh"
 #include "dhop_kernel.cuh"
+#include "layout.cuh"
 
 namespace gbdw {
 
@@ -131,7 +132,7 @@ __global__ void k_gauge_import(const SRC* src, int64_t nsite, int nsimd, void* d
 // Reference spinor (complex SRC, nsimd lanes, Ls slices) -> right-hand side `rhs` of a field.
 template <class SRC, int P>
 __global__ void k_spinor_import(const SRC* src, int64_t nsite, int Ls, int nsimd, int nrhs, int rhs, void* dst,
-                                float* norm) {
+                                float* norm, int LsP) {
   const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;  // (site, s)
   if (i >= nsite * Ls) return;
   const int64_t site = i / Ls;
@@ -151,39 +152,29 @@ __global__ void k_spinor_import(const SRC* src, int64_t nsite, int Ls, int nsimd
     for (int k = 0; k < 24; ++k) m = fmaxf(m, fabsf(float(v[k])));
     const float sc = m > 0.f ? 1.f / m : 0.f;
     norm[site * LsE + e] = m;
-    for (int k = 0; k < 12; ++k)
-      ((__half2*)dst)[(site * 12 + k) * LsE + e] = __floats2half2_rn(float(v[2 * k]) * sc, float(v[2 * k + 1]) * sc);
+    for (int k = 0; k < 12; ++k) Elem<GBDW_F16>::st(dst, site * 12 + k, e, LsP, float(v[2 * k]) * sc, float(v[2 * k + 1]) * sc);
   } else {
-    for (int k = 0; k < 12; ++k) {
-      const int64_t d = (site * 12 + k) * LsE + e;
-      if (P == GBDW_F64) ((double2*)dst)[d] = make_double2(v[2 * k], v[2 * k + 1]);
-      else ((float2*)dst)[d] = make_float2(float(v[2 * k]), float(v[2 * k + 1]));
-    }
+    for (int k = 0; k < 12; ++k) Elem<P>::st(dst, site * 12 + k, e, LsP, v[2 * k], v[2 * k + 1]);
   }
 }
 
 template <int P>
-__device__ __forceinline__ void read_entry(const void* d, const float* norm, int64_t idx, int64_t nidx, double& re,
-                                           double& im) {
-  if (P == GBDW_F64) {
-    const double2 a = ((const double2*)d)[idx];
-    re = a.x;
-    im = a.y;
-  } else if (P == GBDW_F32) {
-    const float2 a = ((const float2*)d)[idx];
-    re = a.x;
-    im = a.y;
-  } else {
-    const float2 a = __half22float2(((const __half2*)d)[idx]);
+__device__ __forceinline__ void read_entry(const void* d, const float* norm, int64_t row, int e, int LsP, int64_t nidx,
+                                           double& re, double& im) {
+  const auto a = Elem<P>::ld(d, row, e, LsP);
+  if (P == GBDW_F16) {
     const float n = norm[nidx];
-    re = double(a.x * n);
-    im = double(a.y * n);
+    re = double(float(a.r) * n);
+    im = double(float(a.i) * n);
+  } else {
+    re = double(a.r);
+    im = double(a.i);
   }
 }
 
 template <class DST, int P>
 __global__ void k_spinor_export(const void* srcd, const float* norm, int64_t nsite, int Ls, int nsimd, int nrhs,
-                                int rhs, DST* dst) {
+                                int rhs, DST* dst, int LsP) {
   const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (i >= nsite * Ls) return;
   const int64_t site = i / Ls;
@@ -194,7 +185,7 @@ __global__ void k_spinor_export(const void* srcd, const float* norm, int64_t nsi
   const int e = s * nrhs + rhs;
   for (int k = 0; k < 12; ++k) {
     double re, im;
-    read_entry<P>(srcd, norm, (site * 12 + k) * LsE + e, site * LsE + e, re, im);
+    read_entry<P>(srcd, norm, site * 12 + k, e, LsP, site * LsE + e, re, im);
     const int64_t j = ((o * Ls + s) * 12 + k) * nsimd + lane;
     dst[2 * j] = DST(re);
     dst[2 * j + 1] = DST(im);
@@ -203,26 +194,22 @@ __global__ void k_spinor_export(const void* srcd, const float* norm, int64_t nsi
 
 // Field-to-field precision conversion, one thread per 5D entry (site, e).
 template <int PS, int PD>
-__global__ void k_field_convert(const void* src, const float* snorm, void* dst, float* dnorm, int64_t nsite, int LsE) {
+__global__ void k_field_convert(const void* src, const float* snorm, void* dst, float* dnorm, int64_t nsite, int LsE,
+                                int LsPs, int LsPd) {
   const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (i >= nsite * LsE) return;
   const int64_t site = i / LsE;
   const int e = int(i - site * LsE);
   double v[24];
-  for (int k = 0; k < 12; ++k) read_entry<PS>(src, snorm, (site * 12 + k) * LsE + e, i, v[2 * k], v[2 * k + 1]);
+  for (int k = 0; k < 12; ++k) read_entry<PS>(src, snorm, site * 12 + k, e, LsPs, i, v[2 * k], v[2 * k + 1]);
   if (PD == GBDW_F16) {
     float m = 0.f;
     for (int k = 0; k < 24; ++k) m = fmaxf(m, fabsf(float(v[k])));
     const float sc = m > 0.f ? 1.f / m : 0.f;
     dnorm[i] = m;
-    for (int k = 0; k < 12; ++k)
-      ((__half2*)dst)[(site * 12 + k) * LsE + e] = __floats2half2_rn(float(v[2 * k]) * sc, float(v[2 * k + 1]) * sc);
+    for (int k = 0; k < 12; ++k) Elem<GBDW_F16>::st(dst, site * 12 + k, e, LsPd, float(v[2 * k]) * sc, float(v[2 * k + 1]) * sc);
   } else {
-    for (int k = 0; k < 12; ++k) {
-      const int64_t d = (site * 12 + k) * LsE + e;
-      if (PD == GBDW_F64) ((double2*)dst)[d] = make_double2(v[2 * k], v[2 * k + 1]);
-      else ((float2*)dst)[d] = make_float2(float(v[2 * k]), float(v[2 * k + 1]));
-    }
+    for (int k = 0; k < 12; ++k) Elem<PD>::st(dst, site * 12 + k, e, LsPd, v[2 * k], v[2 * k + 1]);
   }
 }
 
@@ -235,7 +222,8 @@ int field_convert(gbdw_field* dst, const gbdw_field* src) {
   if (n == 0) return GBDW_OK;
   const int t = 256;
 #define GBDW_CONV(PS, PD) \
-  k_field_convert<PS, PD><<<nblk(n, t), t, 0, stream()>>>(src->d, src->norm, dst->d, dst->norm, src->lat->nsite, src->LsE)
+  k_field_convert<PS, PD><<<nblk(n, t), t, 0, stream()>>>(src->d, src->norm, dst->d, dst->norm, src->lat->nsite, src->LsE, \
+                                                          src->LsP, dst->LsP)
   const int key = src->prec * 4 + dst->prec;
   switch (key) {
     case GBDW_F64 * 4 + GBDW_F32: GBDW_CONV(GBDW_F64, GBDW_F32); break;
@@ -467,6 +455,7 @@ int gbdw_field_create(gbdw_field** f, const gbdw_lattice* lat, int prec, int nrh
   F->prec = prec;
   F->nrhs = nrhs;
   F->LsE = lat->Ls * nrhs;
+  F->LsP = padded_slices(prec, F->LsE);
   F->norm = nullptr;
   F->bytes = size_t(F->elems()) * spinor_elem_bytes(prec);
   cudaError_t e = cudaMalloc(&F->d, F->bytes);
@@ -515,7 +504,7 @@ int gbdw_field_import(gbdw_field* f, int rhs, const void* src, int src_prec) {
   const int t = 256;
 #define GBDW_SI(SRC, P)                                                                                      \
   k_spinor_import<SRC, P><<<nblk(n5, t), t, 0, stream()>>>((const SRC*)dsrc, L->nsite, L->Ls, L->nsimd, f->nrhs, rhs, \
-                                                          f->d, f->norm)
+                                                          f->d, f->norm, f->LsP)
   if (src_prec == GBDW_F64) {
     if (f->prec == GBDW_F64) GBDW_SI(double, GBDW_F64);
     else if (f->prec == GBDW_F32) GBDW_SI(double, GBDW_F32);
@@ -549,7 +538,8 @@ int gbdw_field_export(const gbdw_field* f, int rhs, void* dst, int dst_prec) {
   }
   const int t = 256;
 #define GBDW_SE(DST, P) \
-  k_spinor_export<DST, P><<<nblk(n5, t), t, 0, stream()>>>(f->d, f->norm, L->nsite, L->Ls, L->nsimd, f->nrhs, rhs, (DST*)ddst)
+  k_spinor_export<DST, P><<<nblk(n5, t), t, 0, stream()>>>(f->d, f->norm, L->nsite, L->Ls, L->nsimd, f->nrhs, rhs, \
+                                                           (DST*)ddst, f->LsP)
   if (dst_prec == GBDW_F64) {
     if (f->prec == GBDW_F64) GBDW_SE(double, GBDW_F64);
     else if (f->prec == GBDW_F32) GBDW_SE(double, GBDW_F32);

@@ -4,6 +4,7 @@
 // i.i.d. N(0,1) real and imaginary parts for spinors) but with CUDA's log/sincos, so the bits
 // differ from gbdw_generate_*; parity tests use the host generator.
 #include "common.cuh"
+#include "layout.cuh"
 
 namespace gbdw {
 namespace {
@@ -26,7 +27,7 @@ __device__ __forceinline__ double2 gauss2(uint64_t& st) {
 }
 
 __global__ void k_field_gaussian(void* d, float* norm, int prec, int64_t nsite, int Ls, int nrhs, int rhs,
-                                 uint64_t seed) {
+                                 uint64_t seed, int LsP) {
   const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;  // (site, s)
   if (i >= nsite * Ls) return;
   const int64_t site = i / Ls;
@@ -44,10 +45,9 @@ __global__ void k_field_gaussian(void* d, float* norm, int prec, int64_t nsite, 
   const float sc = m > 0.f ? 1.f / m : 0.f;
   if (prec == GBDW_F16) norm[site * LsE + e] = m;
   for (int k = 0; k < 12; ++k) {
-    const int64_t idx = (site * 12 + k) * LsE + e;
-    if (prec == GBDW_F64) ((double2*)d)[idx] = v[k];
-    else if (prec == GBDW_F32) ((float2*)d)[idx] = make_float2(float(v[k].x), float(v[k].y));
-    else ((__half2*)d)[idx] = __floats2half2_rn(float(v[k].x) * sc, float(v[k].y) * sc);
+    if (prec == GBDW_F64) Elem<GBDW_F64>::st(d, site * 12 + k, e, LsP, v[k].x, v[k].y);
+    else if (prec == GBDW_F32) Elem<GBDW_F32>::st(d, site * 12 + k, e, LsP, float(v[k].x), float(v[k].y));
+    else Elem<GBDW_F16>::st(d, site * 12 + k, e, LsP, float(v[k].x) * sc, float(v[k].y) * sc);
   }
 }
 
@@ -140,7 +140,7 @@ int gbdw_field_gaussian(gbdw_field* f, int rhs, uint64_t seed) {
   if (int st = ensure_device()) return st;
   const int64_t n = f->lat->nsite * f->lat->Ls;
   k_field_gaussian<<<nb(n, 256), 256, 0, stream()>>>(f->d, f->norm, f->prec, f->lat->nsite, f->lat->Ls, f->nrhs, rhs,
-                                                     seed * 0x9E3779B97F4A7C15ull + uint64_t(rhs));
+                                                     seed * 0x9E3779B97F4A7C15ull + uint64_t(rhs), f->LsP);
   GBDW_LAUNCHED();
   return GBDW_OK;
 }

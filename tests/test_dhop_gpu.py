@@ -120,8 +120,8 @@ def test_table_out_of_range_is_rejected(gpu):
     assert e.value.status == 4
 
 
-SHAPES = {gb.F32: [(0, s, 4) for s in (1, 2, 4)] + [(1, s, st) for s in (1, 2) for st in (2, 4)],
-          gb.F64: [(0, s, 4) for s in (1, 2)] + [(1, s, st) for s in (1, 2) for st in (2, 4)]}
+SHAPES = {gb.F32: [(0, s, 4) for s in (1, 2, 4)] + [(f, s, st) for f in (1, 2) for s in (1, 2) for st in (2, 4)],
+          gb.F64: [(0, s, 4) for s in (1, 2)] + [(f, s, st) for f in (1, 2) for s in (1, 2) for st in (2, 4)]}
 
 
 @pytest.mark.parametrize("prec", [gb.F32, gb.F64])
@@ -143,7 +143,7 @@ def test_every_launch_shape(gpu, prec, threads, Ls):
             try:
                 gb.tune_set(g, x, threads, spt, form, stages)
             except gb.GbdwError:
-                assert form == 1  # a staged ring that does not fit in shared memory
+                assert form != 0  # a staged ring that does not fit (or a site wider than a warp)
                 continue
             y.zero()
             gb.dhop(g, y, x, dag)
