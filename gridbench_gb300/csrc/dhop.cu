@@ -113,9 +113,7 @@ bool tma_shape(int prec, int LsE, DhopLaunch L, int* NS, int* threads, size_t* s
     // one ring per warp: a warp owns 32/Tps whole sites
     if (Tps > 32 || L.threads % 32 != 0 || L.threads > 256) return false;
     const int nsw = 32 / Tps, W = L.threads / 32;
-    const bool paired = prec != GBDW_F64 && L.spt % 2 == 0;  // links expanded for the pair arithmetic
-    const size_t per_warp = size_t(L.stages) * nsw * blk + nsw * lb + (paired ? size_t(nsw) * 8 * 9 * 16 : 0) +
-                            ((size_t(L.stages + 1) * 8 + 15) & ~size_t(15));
+    const size_t per_warp = size_t(L.stages) * nsw * blk + nsw * lb + ((size_t(L.stages + 1) * 8 + 15) & ~size_t(15));
     if (W * per_warp > max_dynamic_smem()) return false;
     *NS = W * nsw;
     *threads = L.threads;

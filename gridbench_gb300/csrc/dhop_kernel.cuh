@@ -231,75 +231,6 @@ __device__ __forceinline__ void hop_leg_pairs(const cpx<float> (&u)[3][3], const
     }
 }
 
-// Row r of a pre-broadcast link (e[c] = {Re, Re, Im, Im} of U[r][c]) times h; nhi holds -Im h.
-__device__ __forceinline__ cp2 su3_row2b(const float4 (&e)[3], const cp2 (&h)[3], const float2 (&nhi)[3]) {
-  cp2 o;
-  o.r = __fmul2_rn(make_float2(e[0].x, e[0].y), h[0].r);
-  o.i = __fmul2_rn(make_float2(e[0].x, e[0].y), h[0].i);
-  o.r = __ffma2_rn(make_float2(e[0].z, e[0].w), nhi[0], o.r);
-  o.i = __ffma2_rn(make_float2(e[0].z, e[0].w), h[0].r, o.i);
-#pragma unroll
-  for (int c = 1; c < 3; ++c) {
-    o.r = __ffma2_rn(make_float2(e[c].x, e[c].y), h[c].r, o.r);
-    o.i = __ffma2_rn(make_float2(e[c].x, e[c].y), h[c].i, o.i);
-    o.r = __ffma2_rn(make_float2(e[c].z, e[c].w), nhi[c], o.r);
-    o.i = __ffma2_rn(make_float2(e[c].z, e[c].w), h[c].r, o.i);
-  }
-  return o;
-}
-
-// The same leg as hop_leg_pairs with the link taken pre-broadcast from shared memory
-// (9 float4 {Re, Re, Im, Im}), so no register pair has to be built from a scalar.
-template <int PIN, int DAG, int NP, int L>
-__device__ __forceinline__ void hop_leg_pairs_b(const float4* ul, const void* in, int64_t row0, int e0, int LsP,
-                                                const float* nrm, cp2 (&acc)[NP][12]) {
-  using S = LegSpin<DAG ? (L ^ 4) : L>;
-  cp2 h0[NP][3], h1[NP][3];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    cp2 x[NP], y[NP], z[NP], w[NP];
-    Vec<PIN, 2 * NP, true>::load_pairs(in, row0 + 0 * 3 + c, e0, LsP, x);
-    Vec<PIN, 2 * NP, true>::load_pairs(in, row0 + S::A * 3 + c, e0, LsP, y);
-    Vec<PIN, 2 * NP, true>::load_pairs(in, row0 + 1 * 3 + c, e0, LsP, z);
-    Vec<PIN, 2 * NP, true>::load_pairs(in, row0 + S::B * 3 + c, e0, LsP, w);
-#pragma unroll
-    for (int q = 0; q < NP; ++q) {
-      h0[q][c] = cadd2(x[q], cunit2<S::C0>(y[q]));
-      h1[q][c] = cadd2(z[q], cunit2<S::C1>(w[q]));
-    }
-  }
-  if constexpr (PIN == GBDW_F16) {
-#pragma unroll
-    for (int q = 0; q < NP; ++q) {
-      const float2 nr = reinterpret_cast<const float2*>(nrm)[q];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        h0[q][c] = {__fmul2_rn(h0[q][c].r, nr), __fmul2_rn(h0[q][c].i, nr)};
-        h1[q][c] = {__fmul2_rn(h1[q][c].r, nr), __fmul2_rn(h1[q][c].i, nr)};
-      }
-    }
-  }
-#pragma unroll
-  for (int q = 0; q < NP; ++q) {
-    float2 n0[3], n1[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      n0[c] = neg2(h0[q][c].i);
-      n1[c] = neg2(h1[q][c].i);
-    }
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-      const float4 e[3] = {ul[r * 3 + 0], ul[r * 3 + 1], ul[r * 3 + 2]};
-      const cp2 u0 = su3_row2b(e, h0[q], n0);
-      const cp2 u1 = su3_row2b(e, h1[q], n1);
-      acc[q][0 * 3 + r] = cadd2(acc[q][0 * 3 + r], u0);
-      acc[q][1 * 3 + r] = cadd2(acc[q][1 * 3 + r], u1);
-      acc[q][S::A * 3 + r] = cadd2(acc[q][S::A * 3 + r], cunit2<conj_unit<S::C0>::v>(u0));
-      acc[q][S::B * 3 + r] = cadd2(acc[q][S::B * 3 + r], cunit2<conj_unit<S::C1>::v>(u1));
-    }
-  }
-}
-
 // One leg on N single slices (FP64, or N == 1).
 template <int PIN, int DAG, int N, int L, bool SMEM, class T>
 __device__ __forceinline__ void hop_leg_scalar(const cpx<T> (&u)[3][3], const void* in, int64_t row0, int e0, int LsP,

@@ -182,17 +182,13 @@ __global__ void __launch_bounds__(256) k_dhop_tma(const DhopParams p, int NS) {
 // block and its own mbarriers, and synchronises only with __syncwarp.  No CTA-wide barrier
 // sits between the legs, so a warp that finished its leg refills its buffer at once.
 // Shared memory per warp: STAGES*NSW*(blk+nblk) + NSW*links + (STAGES+1)*8 bytes.
-// Bytes of one site's links expanded for the pair arithmetic: 8 legs x 9 x {Re,Re,Im,Im}.
-constexpr unsigned kXLinkBytes = 8u * 9u * 16u;
-
 template <int PIN, int GP>
-__host__ __device__ inline unsigned tmaw_warp_bytes(int NSW, int LsE, int LsP, int STAGES, bool paired) {
+__host__ __device__ inline unsigned tmaw_warp_bytes(int NSW, int LsE, int LsP, int STAGES) {
   const unsigned esz = PIN == GBDW_F64 ? 16u : PIN == GBDW_F32 ? 8u : 4u;
   const unsigned blk = 12u * unsigned(LsP) * esz + (PIN == GBDW_F16 ? 4u * unsigned(LsE) : 0u);
   const unsigned lb = GP == GBDW_F64 ? 8u * 144u : GP == GBDW_F32 ? 8u * 72u : 8u * 24u;
   // barrier area padded to 16 bytes so every warp's buffers stay 16-byte aligned for TMA
-  return unsigned(STAGES) * unsigned(NSW) * blk + unsigned(NSW) * lb + (paired ? unsigned(NSW) * kXLinkBytes : 0u) +
-         ((unsigned(STAGES + 1) * 8u + 15u) & ~15u);
+  return unsigned(STAGES) * unsigned(NSW) * blk + unsigned(NSW) * lb + ((unsigned(STAGES + 1) * 8u + 15u) & ~15u);
 }
 
 template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int STAGES>
@@ -206,12 +202,10 @@ __global__ void __launch_bounds__(256) k_dhop_tmaw(const DhopParams p) {
   const unsigned nblk = (PIN == GBDW_F16) ? 4u * unsigned(LsE) : 0u;
   const unsigned stage = unsigned(NSW) * (blk + nblk);
   constexpr unsigned LB = 8 * LinkIO<GP>::bytes;  // a site's 8 links
-  constexpr bool PAIRED = Acc<PIN, N>::paired;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  unsigned char* wbase = smem + warp * tmaw_warp_bytes<PIN, GP>(NSW, LsE, LsP, STAGES, PAIRED);
+  unsigned char* wbase = smem + warp * tmaw_warp_bytes<PIN, GP>(NSW, LsE, LsP, STAGES);
   unsigned char* links = wbase + STAGES * stage;
-  float4* xlinks = reinterpret_cast<float4*>(links + NSW * LB);  // pair path only
-  uint64_t* bars = reinterpret_cast<uint64_t*>(links + NSW * LB + (PAIRED ? NSW * kXLinkBytes : 0u));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(links + NSW * LB);
   const int64_t site0 = (int64_t(blockIdx.x) * (blockDim.x >> 5) + warp) * NSW;
   const int nvalid = int(max(int64_t(0), min(int64_t(NSW), p.nsite - site0)));
   const int sl = lane / Tps;
@@ -256,20 +250,6 @@ __global__ void __launch_bounds__(256) k_dhop_tmaw(const DhopParams p) {
 
     failed = __any_sync(0xffffffffu, !mbar_wait_bounded(&bars[STAGES], 0, kWaitLimitNs));
     const unsigned char* my_links = links + (active ? sl : 0) * LB;
-    if constexpr (PAIRED) {
-      // broadcast every link entry once per warp: lane t expands (site t/8, leg t%8), F16/BF16
-      // rows 2 rebuilt here instead of in every thread
-      if (!failed) {
-        for (int t = lane; t < nvalid * 8; t += 32) {
-          cpx<float> u[3][3];
-          LinkIO<GP>::template load<true>(links + (t >> 3) * LB, t & 7, u);
-          float4* dst = xlinks + t * 9;
-#pragma unroll
-          for (int k = 0; k < 9; ++k) dst[k] = make_float4(u[k / 3][k % 3].r, u[k / 3][k % 3].r, u[k / 3][k % 3].i, u[k / 3][k % 3].i);
-        }
-      }
-      __syncwarp();
-    }
 #define GBDW_TMAW_LEG(L)                                                                                   \
   if (!failed) {                                                                                           \
     const int st = (L) % STAGES;                                                                           \
@@ -278,15 +258,10 @@ __global__ void __launch_bounds__(256) k_dhop_tmaw(const DhopParams p) {
       consumed = (L) + 1;                                                                                  \
       const unsigned char* base = wbase + st * stage;                                                      \
       if (active) {                                                                                        \
-        const float* nrm_ = reinterpret_cast<const float*>(base + NSW * blk + sl * nblk) + s0;             \
-        if constexpr (PAIRED) {                                                                            \
-          hop_leg_pairs_b<PIN, DAG, N / 2, L>(xlinks + (sl * 8 + (L)) * 9, base + sl * blk, 0, s0, LsP,    \
-                                              nrm_, acc.v);                                                \
-        } else {                                                                                           \
-          cpx<T> u[3][3];                                                                                  \
-          LinkIO<GP>::template load<true>(my_links, (L), u);                                               \
-          hop_leg<PIN, DAG, N, L, true>(u, base + sl * blk, 0, s0, LsP, nrm_, acc);                        \
-        }                                                                                                  \
+        cpx<T> u[3][3];                                                                                    \
+        LinkIO<GP>::template load<true>(my_links, (L), u);                                                 \
+        hop_leg<PIN, DAG, N, L, true>(u, base + sl * blk, 0, s0, LsP,                                      \
+                                      reinterpret_cast<const float*>(base + NSW * blk + sl * nblk) + s0, acc); \
       }                                                                                                    \
       if ((L) + STAGES < 8) {                                                                              \
         __syncwarp();                                                                                      \
