@@ -192,6 +192,58 @@ __global__ void k_spinor_export(const void* srcd, const float* norm, int64_t nsi
   }
 }
 
+// Site-block conversions for the common case Nsimd = 1, one right-hand side: a site's spinor
+// is one contiguous run of 12*Ls entries in both layouts, so one warp per site moves it with
+// coalesced 16-byte accesses through shared memory and permutes it there.
+template <class SRC, int P>
+__global__ void k_import_blocks(const SRC* __restrict__ src, int64_t nsite, int Ls, void* dst, float* norm, int LsP) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t site = int64_t(blockIdx.x) * (blockDim.x >> 5) + warp;
+  if (site >= nsite) return;
+  const int nreal = 24 * Ls;  // reals of the site block
+  SRC* buf = reinterpret_cast<SRC*>(sm) + size_t(warp) * nreal;
+  const SRC* s = src + site * nreal;
+  constexpr int V = 16 / sizeof(SRC);  // reals per 16-byte vector
+  for (int i = lane; i < nreal / V; i += 32) reinterpret_cast<uint4*>(buf)[i] = __ldg(reinterpret_cast<const uint4*>(s) + i);
+  __syncwarp();
+  for (int e = lane; e < Ls; e += 32) {
+    const SRC* v = buf + e * 24;
+    if (P == GBDW_F16) {
+      float m = 0.f;
+      for (int k = 0; k < 24; ++k) m = fmaxf(m, fabsf(float(v[k])));
+      const float sc = m > 0.f ? 1.f / m : 0.f;
+      norm[site * Ls + e] = m;
+      for (int k = 0; k < 12; ++k) Elem<GBDW_F16>::st(dst, site * 12 + k, e, LsP, float(v[2 * k]) * sc, float(v[2 * k + 1]) * sc);
+    } else {
+      for (int k = 0; k < 12; ++k) Elem<P>::st(dst, site * 12 + k, e, LsP, v[2 * k], v[2 * k + 1]);
+    }
+  }
+}
+
+template <class DST, int P>
+__global__ void k_export_blocks(const void* __restrict__ srcd, const float* __restrict__ norm, int64_t nsite, int Ls,
+                                DST* __restrict__ dst, int LsP) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t site = int64_t(blockIdx.x) * (blockDim.x >> 5) + warp;
+  if (site >= nsite) return;
+  const int nreal = 24 * Ls;
+  DST* buf = reinterpret_cast<DST*>(sm) + size_t(warp) * nreal;
+  for (int e = lane; e < Ls; e += 32) {
+    const float n = (P == GBDW_F16) ? __ldg(norm + site * Ls + e) : 1.f;
+    for (int k = 0; k < 12; ++k) {
+      const auto a = Elem<P>::ld(srcd, site * 12 + k, e, LsP);
+      buf[e * 24 + 2 * k] = (P == GBDW_F16) ? DST(float(a.r) * n) : DST(a.r);
+      buf[e * 24 + 2 * k + 1] = (P == GBDW_F16) ? DST(float(a.i) * n) : DST(a.i);
+    }
+  }
+  __syncwarp();
+  constexpr int V = 16 / sizeof(DST);
+  uint4* d = reinterpret_cast<uint4*>(dst + site * nreal);
+  for (int i = lane; i < nreal / V; i += 32) d[i] = reinterpret_cast<const uint4*>(buf)[i];
+}
+
 // Field-to-field precision conversion, one thread per 5D entry (site, e).
 template <int PS, int PD>
 __global__ void k_field_convert(const void* src, const float* snorm, void* dst, float* dnorm, int64_t nsite, int LsE,
@@ -502,6 +554,25 @@ int gbdw_field_import(gbdw_field* f, int rhs, const void* src, int src_prec) {
   const void* dsrc = nullptr;
   if (int st = stage_in(src, bytes, 5, &dsrc)) return st;
   const int t = 256;
+  // site blocks: 4 warps per CTA, 24*Ls reals of shared memory per warp
+  const size_t blk_smem = 4 * size_t(24) * L->Ls * (src_prec == GBDW_F64 ? 8 : 4);
+  if (L->nsimd == 1 && f->nrhs == 1 && blk_smem <= 48 * 1024 && (uintptr_t(dsrc) & 15) == 0) {
+    const unsigned nb = unsigned((L->nsite + 3) / 4);
+#define GBDW_IB(SRC, P) \
+  k_import_blocks<SRC, P><<<nb, 128, blk_smem, stream()>>>((const SRC*)dsrc, L->nsite, L->Ls, f->d, f->norm, f->LsP)
+    if (src_prec == GBDW_F64) {
+      if (f->prec == GBDW_F64) GBDW_IB(double, GBDW_F64);
+      else if (f->prec == GBDW_F32) GBDW_IB(double, GBDW_F32);
+      else GBDW_IB(double, GBDW_F16);
+    } else {
+      if (f->prec == GBDW_F64) GBDW_IB(float, GBDW_F64);
+      else if (f->prec == GBDW_F32) GBDW_IB(float, GBDW_F32);
+      else GBDW_IB(float, GBDW_F16);
+    }
+#undef GBDW_IB
+    GBDW_LAUNCHED();
+    return GBDW_OK;
+  }
 #define GBDW_SI(SRC, P)                                                                                      \
   k_spinor_import<SRC, P><<<nblk(n5, t), t, 0, stream()>>>((const SRC*)dsrc, L->nsite, L->Ls, L->nsimd, f->nrhs, rhs, \
                                                           f->d, f->norm, f->LsP)
@@ -537,6 +608,22 @@ int gbdw_field_export(const gbdw_field* f, int rhs, void* dst, int dst_prec) {
     }
   }
   const int t = 256;
+  const size_t blk_smem = 4 * size_t(24) * L->Ls * (dst_prec == GBDW_F64 ? 8 : 4);
+  if (L->nsimd == 1 && f->nrhs == 1 && blk_smem <= 48 * 1024 && (uintptr_t(ddst) & 15) == 0) {
+    const unsigned nb = unsigned((L->nsite + 3) / 4);
+#define GBDW_EB(DST, P) \
+  k_export_blocks<DST, P><<<nb, 128, blk_smem, stream()>>>(f->d, f->norm, L->nsite, L->Ls, (DST*)ddst, f->LsP)
+    if (dst_prec == GBDW_F64) {
+      if (f->prec == GBDW_F64) GBDW_EB(double, GBDW_F64);
+      else if (f->prec == GBDW_F32) GBDW_EB(double, GBDW_F32);
+      else GBDW_EB(double, GBDW_F16);
+    } else {
+      if (f->prec == GBDW_F64) GBDW_EB(float, GBDW_F64);
+      else if (f->prec == GBDW_F32) GBDW_EB(float, GBDW_F32);
+      else GBDW_EB(float, GBDW_F16);
+    }
+#undef GBDW_EB
+  } else {
 #define GBDW_SE(DST, P) \
   k_spinor_export<DST, P><<<nblk(n5, t), t, 0, stream()>>>(f->d, f->norm, L->nsite, L->Ls, L->nsimd, f->nrhs, rhs, \
                                                            (DST*)ddst, f->LsP)
@@ -550,6 +637,7 @@ int gbdw_field_export(const gbdw_field* f, int rhs, void* dst, int dst_prec) {
     else GBDW_SE(float, GBDW_F16);
   }
 #undef GBDW_SE
+  }
   GBDW_LAUNCHED();
   if (!dev) {
     GBDW_CUDA(cudaMemcpyAsync(dst, ddst, bytes, cudaMemcpyDeviceToHost, stream()));
