@@ -483,33 +483,6 @@ __device__ __forceinline__ void dwf_epilogue(const DhopParams& p, int64_t site, 
 }
 
 // ------------------------------------------------------------------ kernels
-__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
-
-// Byte address of the data of slices e0.. of row `row` (e0 even for F32/F16).
-template <int P>
-__device__ __forceinline__ const unsigned char* row_ptr(const void* base, int64_t row, int e0, int LsP) {
-  if constexpr (P == GBDW_F64) return (const unsigned char*)base + (row * LsP + e0) * 16;
-  else return (const unsigned char*)base + (row * 2 * int64_t(LsP) + 2 * e0) * (P == GBDW_F32 ? 4 : 2);
-}
-
-// Pulls leg L's neighbour rows (and link, F16 norms) of this thread into L1 ahead of use.  One
-// thread per 128-byte line issues the prefetch, so the cost is a few instructions per leg
-// and no registers, while the loads of that leg later hit L1 instead of waiting on L2.
-template <int PIN, int GP, int N>
-__device__ __forceinline__ void prefetch_leg(const DhopParams& p, unsigned site, uint32_t n, int L, int s0) {
-  constexpr int CB = (PIN == GBDW_F64 ? 16 : PIN == GBDW_F32 ? 8 : 4) * N;  // bytes of a thread per row
-  constexpr int TPL = CB >= 128 ? 1 : 128 / CB;                              // threads per 128-byte line
-  const int g = s0 / N;
-  if (g % TPL == 0) {
-#pragma unroll
-    for (int k = 0; k < 12; ++k) prefetch_l1(row_ptr<PIN>(p.in, int64_t(n) * 12 + k, s0, p.LsP));
-  }
-  if (g == 0) {
-    prefetch_l1((const unsigned char*)p.U + (size_t(site) * 8 + L) * LinkIO<GP>::bytes);
-    if constexpr (PIN == GBDW_F16) prefetch_l1(p.in_norm + int64_t(n) * p.LsE);
-  }
-}
-
 // Hopping sum for one thread: site and first slice s0 of N consecutive slices.
 template <int PIN, int GP, int DAG, int N>
 __device__ __forceinline__ void dhop_thread(const DhopParams& p, unsigned site, int s0,
@@ -517,15 +490,10 @@ __device__ __forceinline__ void dhop_thread(const DhopParams& p, unsigned site, 
   using T = typename Arith<PIN>::T;
   Acc<PIN, N> acc;
   acc.zero();
-  const uint4* nbv = reinterpret_cast<const uint4*>(p.nbr4 + size_t(site) * 8);
-  const uint4 na = __ldg(nbv), nc = __ldg(nbv + 1);
-  const uint32_t nb[8] = {na.x, na.y, na.z, na.w, nc.x, nc.y, nc.z, nc.w};
-  prefetch_leg<PIN, GP, N>(p, site, nb[1], 1, s0);
-  prefetch_leg<PIN, GP, N>(p, site, nb[2], 2, s0);
+  const uint32_t* nb = p.nbr4 + size_t(site) * 8;
 #define GBDW_LEG(L)                                                                                    \
   {                                                                                                    \
-    if (L >= 1 && L + 2 < 8) prefetch_leg<PIN, GP, N>(p, site, nb[(L + 2) & 7], (L + 2) & 7, s0);      \
-    const int64_t n = nb[L];                                                                           \
+    const int64_t n = __ldg(nb + L);                                                                   \
     cpx<T> u[3][3];                                                                                    \
     LinkIO<GP>::load(p.U, size_t(site) * 8 + L, u);                                                    \
     hop_leg<PIN, DAG, N, L, false>(u, p.in, n * 12, s0, p.LsP, p.in_norm + n * p.LsE + s0, acc);       \

@@ -49,11 +49,14 @@ __device__ __forceinline__ uint64_t global_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-// Waits for the phase with the given parity to complete; false after limit_ns.
+// Waits for the phase with the given parity to complete; false after limit_ns.  Between
+// polls the warp sleeps briefly, so a waiting warp stops taking issue slots from the warps
+// that have data to work on.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, uint64_t limit_ns) {
   if (mbar_try(bar, parity)) return true;
   const uint64_t t0 = global_ns();
   for (;;) {
+    __nanosleep(64);
     if (mbar_try(bar, parity)) return true;
     if (global_ns() - t0 > limit_ns) return false;
   }
