@@ -189,6 +189,20 @@ __device__ __forceinline__ cp2 su3_row2(const cpx<float> (&u)[3], const cp2 (&h)
 
 // One leg on NP slice pairs: the neighbour's rows start at row0 of `in` (global or smem);
 // nrm points at the F16 norms of its first slice.
+// x + c*y on stored FP16 pairs (Re pair in .x, Im pair in .y), c a unit; both operands share
+// the site norm, so the sum is formed before the conversion to FP32.
+template <int C>
+__device__ __forceinline__ cp2 hproj(uint2 x, uint2 y) {
+  const __half2 xr = *reinterpret_cast<__half2*>(&x.x), xi = *reinterpret_cast<__half2*>(&x.y);
+  const __half2 yr = *reinterpret_cast<__half2*>(&y.x), yi = *reinterpret_cast<__half2*>(&y.y);
+  __half2 r, i;
+  if constexpr (C == 0) { r = __hadd2(xr, yr); i = __hadd2(xi, yi); }
+  else if constexpr (C == 1) { r = __hsub2(xr, yr); i = __hsub2(xi, yi); }
+  else if constexpr (C == 2) { r = __hsub2(xr, yi); i = __hadd2(xi, yr); }   // + i y
+  else { r = __hadd2(xr, yi); i = __hsub2(xi, yr); }                         // - i y
+  return {__half22float2(r), __half22float2(i)};
+}
+
 template <int PIN, int DAG, int NP, int L, bool SMEM>
 __device__ __forceinline__ void hop_leg_pairs(const cpx<float> (&u)[3][3], const void* in, int64_t row0, int e0,
                                               int LsP, const float* nrm, cp2 (&acc)[NP][12]) {
@@ -196,15 +210,28 @@ __device__ __forceinline__ void hop_leg_pairs(const cpx<float> (&u)[3][3], const
   cp2 h0[NP][3], h1[NP][3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    cp2 x[NP], y[NP], z[NP], w[NP];
-    Vec<PIN, 2 * NP, SMEM>::load_pairs(in, row0 + 0 * 3 + c, e0, LsP, x);
-    Vec<PIN, 2 * NP, SMEM>::load_pairs(in, row0 + S::A * 3 + c, e0, LsP, y);
-    Vec<PIN, 2 * NP, SMEM>::load_pairs(in, row0 + 1 * 3 + c, e0, LsP, z);
-    Vec<PIN, 2 * NP, SMEM>::load_pairs(in, row0 + S::B * 3 + c, e0, LsP, w);
+    if constexpr (PIN == GBDW_F16) {
+      uint2 x[NP], y[NP], z[NP], w[NP];
+      Vec<PIN, 2 * NP, SMEM>::load_pairs_raw(in, row0 + 0 * 3 + c, e0, LsP, x);
+      Vec<PIN, 2 * NP, SMEM>::load_pairs_raw(in, row0 + S::A * 3 + c, e0, LsP, y);
+      Vec<PIN, 2 * NP, SMEM>::load_pairs_raw(in, row0 + 1 * 3 + c, e0, LsP, z);
+      Vec<PIN, 2 * NP, SMEM>::load_pairs_raw(in, row0 + S::B * 3 + c, e0, LsP, w);
 #pragma unroll
-    for (int q = 0; q < NP; ++q) {
-      h0[q][c] = cadd2(x[q], cunit2<S::C0>(y[q]));
-      h1[q][c] = cadd2(z[q], cunit2<S::C1>(w[q]));
+      for (int q = 0; q < NP; ++q) {
+        h0[q][c] = hproj<S::C0>(x[q], y[q]);
+        h1[q][c] = hproj<S::C1>(z[q], w[q]);
+      }
+    } else {
+      cp2 x[NP], y[NP], z[NP], w[NP];
+      Vec<PIN, 2 * NP, SMEM>::load_pairs(in, row0 + 0 * 3 + c, e0, LsP, x);
+      Vec<PIN, 2 * NP, SMEM>::load_pairs(in, row0 + S::A * 3 + c, e0, LsP, y);
+      Vec<PIN, 2 * NP, SMEM>::load_pairs(in, row0 + 1 * 3 + c, e0, LsP, z);
+      Vec<PIN, 2 * NP, SMEM>::load_pairs(in, row0 + S::B * 3 + c, e0, LsP, w);
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        h0[q][c] = cadd2(x[q], cunit2<S::C0>(y[q]));
+        h1[q][c] = cadd2(z[q], cunit2<S::C1>(w[q]));
+      }
     }
   }
   if constexpr (PIN == GBDW_F16) {
@@ -504,8 +531,10 @@ __device__ __forceinline__ void dhop_thread(const DhopParams& p, unsigned site, 
 }
 
 // EPI 0: out = Dhop(in) ; EPI 1: out = M(in) (Shamir).  |out|^2 fused when p.partials != 0.
-template <int PIN, int POUT, int GP, int DAG, int N, int EPI>
-__global__ void __launch_bounds__(256) k_dhop(const DhopParams p) {
+// MINB > 0 caps registers so that MINB CTAs of up to 128 threads fit on an SM (more warps,
+// more loads in flight); MINB = 0 leaves the compiler free up to 256 threads.
+template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int MINB = 0>
+__global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1) k_dhop(const DhopParams p) {
   using T = typename Arith<PIN>::T;
   const unsigned G = unsigned(p.LsE) / N;
   const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -559,7 +588,8 @@ __global__ void __launch_bounds__(256) k_dhop_general(const DhopParams p) {
 struct DhopLaunch {
   int threads;     // per CTA (target; the staged kernels round to whole sites)
   int spt;         // slices per thread
-  int mode = 0;    // 0: direct loads, 1: TMA-staged (CTA ring), 2: TMA-staged (one ring per warp)
+  int mode = 0;    // 0: direct loads, 1: TMA-staged (CTA ring), 2: TMA-staged (one ring per warp),
+                   // 3 / 4: forms 0 / 2 with registers capped for 5 CTAs of <= 128 threads per SM
   int stages = 4;  // staged kernels: depth of the leg ring
 };
 

@@ -6,11 +6,11 @@
 
 namespace gbdw {
 
-template <int PIN, int POUT, int GP, int DAG, int N, int EPI>
+template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int MINB = 0>
 int go_direct(const DhopParams& p, DhopLaunch L) {
   const int64_t nthreads = p.nsite * (p.LsE / N);
   const unsigned blocks = unsigned((nthreads + L.threads - 1) / L.threads);
-  k_dhop<PIN, POUT, GP, DAG, N, EPI><<<blocks, L.threads, 0, stream()>>>(p);
+  k_dhop<PIN, POUT, GP, DAG, N, EPI, MINB><<<blocks, L.threads, 0, stream()>>>(p);
   GBDW_LAUNCHED();
   return GBDW_OK;
 }
@@ -38,7 +38,7 @@ int go_tma(const DhopParams& p, DhopLaunch L) {
   return GBDW_OK;
 }
 
-template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int STAGES>
+template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int STAGES, int MINB = 0>
 int go_tmaw(const DhopParams& p, DhopLaunch L) {
   int NS = 0, threads = 0;
   size_t smem = 0;
@@ -46,7 +46,7 @@ int go_tmaw(const DhopParams& p, DhopLaunch L) {
     set_error("warp-staged hopping kernel: no admissible shape for this extent");
     return GBDW_ERR_INVALID;
   }
-  auto kern = k_dhop_tmaw<PIN, POUT, GP, DAG, N, EPI, STAGES>;
+  auto kern = k_dhop_tmaw<PIN, POUT, GP, DAG, N, EPI, STAGES, MINB>;
   static bool opted_in = false;
   if (!opted_in) {
     cudaFuncAttributes fa;
@@ -67,6 +67,10 @@ int by_shape(const DhopParams& p, DhopLaunch L) {
   if (L.mode == 1) {
     if (L.spt == S1) return L.stages == 2 ? go_tma<PIN, POUT, GP, DAG, S1, EPI, 2>(p, L) : go_tma<PIN, POUT, GP, DAG, S1, EPI, 4>(p, L);
     if (L.spt == S2) return L.stages == 2 ? go_tma<PIN, POUT, GP, DAG, S2, EPI, 2>(p, L) : go_tma<PIN, POUT, GP, DAG, S2, EPI, 4>(p, L);
+  } else if (L.mode == 3) {
+    if (L.spt == 2 && PIN != GBDW_F64) return go_direct<PIN, POUT, GP, DAG, 2, EPI, 5>(p, L);
+  } else if (L.mode == 4) {
+    if (L.spt == 2 && PIN != GBDW_F64) return go_tmaw<PIN, POUT, GP, DAG, 2, EPI, 2, 5>(p, L);
   } else if (L.mode == 2) {
     if (L.spt == S1) return L.stages == 2 ? go_tmaw<PIN, POUT, GP, DAG, S1, EPI, 2>(p, L) : go_tmaw<PIN, POUT, GP, DAG, S1, EPI, 4>(p, L);
     if (L.spt == S2) return L.stages == 2 ? go_tmaw<PIN, POUT, GP, DAG, S2, EPI, 2>(p, L) : go_tmaw<PIN, POUT, GP, DAG, S2, EPI, 4>(p, L);

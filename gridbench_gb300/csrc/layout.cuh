@@ -123,6 +123,12 @@ struct Vec {
       }
     }
   }
+  // F16, N even: the stored half2 pairs {Re,Re}, {Im,Im} without conversion
+  __device__ static void load_pairs_raw(const void* b, int64_t row, int e0, int LsP, uint2 (&q)[N / 2]) {
+    const uint2* h = reinterpret_cast<const uint2*>((const unsigned short*)b + row * 2 * int64_t(LsP) + 2 * e0);
+#pragma unroll
+    for (int k = 0; k < N / 2; ++k) q[k] = ldv<SMEM>(h + k);
+  }
   // F64 / F32 stores
   __device__ static void store(void* b, int64_t row, int e0, int LsP, const cpx<T> (&v)[N]) {
     if constexpr (P == GBDW_F64 || N == 1) {
