@@ -533,9 +533,16 @@ __device__ __forceinline__ void dhop_thread(const DhopParams& p, unsigned site, 
 // EPI 0: out = Dhop(in) ; EPI 1: out = M(in) (Shamir).  |out|^2 fused when p.partials != 0.
 // MINB > 0 caps registers so that MINB CTAs of up to 128 threads fit on an SM (more warps,
 // more loads in flight); MINB = 0 leaves the compiler free up to 256 threads.
-template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int MINB = 0>
-__global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1) k_dhop(const DhopParams p) {
+// LSPC > 0: the launch guarantees LsE == LsP == LSPC, so every row offset is a compile-time
+// constant.
+template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int MINB = 0, int LSPC = 0>
+__global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1) k_dhop(const DhopParams p_) {
   using T = typename Arith<PIN>::T;
+  DhopParams p = p_;
+  if constexpr (LSPC > 0) {
+    p.LsE = LSPC;
+    p.LsP = LSPC;
+  }
   const unsigned G = unsigned(p.LsE) / N;
   const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = tid < unsigned(p.nsite) * G;

@@ -10,6 +10,13 @@ template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int MINB = 0>
 int go_direct(const DhopParams& p, DhopLaunch L) {
   const int64_t nthreads = p.nsite * (p.LsE / N);
   const unsigned blocks = unsigned((nthreads + L.threads - 1) / L.threads);
+  if constexpr (PIN == GBDW_F32 && N == 2 && MINB == 0) {
+    if (p.LsE == 16 && p.LsP == 16) {
+      k_dhop<PIN, POUT, GP, DAG, N, EPI, 0, 16><<<blocks, L.threads, 0, stream()>>>(p);
+      GBDW_LAUNCHED();
+      return GBDW_OK;
+    }
+  }
   k_dhop<PIN, POUT, GP, DAG, N, EPI, MINB><<<blocks, L.threads, 0, stream()>>>(p);
   GBDW_LAUNCHED();
   return GBDW_OK;
@@ -46,14 +53,16 @@ int go_tmaw(const DhopParams& p, DhopLaunch L) {
     set_error("warp-staged hopping kernel: no admissible shape for this extent");
     return GBDW_ERR_INVALID;
   }
-  auto kern = k_dhop_tmaw<PIN, POUT, GP, DAG, N, EPI, STAGES, MINB>;
-  static bool opted_in = false;
-  if (!opted_in) {
+  auto kern = (PIN == GBDW_F32 && N == 2 && MINB == 0 && STAGES == 2 && p.LsE == 16 && p.LsP == 16)
+                  ? k_dhop_tmaw<PIN, POUT, GP, DAG, N, EPI, STAGES, MINB, (PIN == GBDW_F32 && N == 2 && MINB == 0 && STAGES == 2) ? 16 : 0>
+                  : k_dhop_tmaw<PIN, POUT, GP, DAG, N, EPI, STAGES, MINB>;
+  static const void* opted_in[2] = {nullptr, nullptr};  // one attribute call per instance
+  if (opted_in[0] != (const void*)kern && opted_in[1] != (const void*)kern) {
     cudaFuncAttributes fa;
     GBDW_CUDA(cudaFuncGetAttributes(&fa, kern));
     const size_t limit = max_dynamic_smem() + 1024 - fa.sharedSizeBytes;
     GBDW_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(limit)));
-    opted_in = true;
+    opted_in[opted_in[0] ? 1 : 0] = (const void*)kern;
   }
   const unsigned blocks = unsigned((p.nsite + NS - 1) / NS);
   kern<<<blocks, threads, smem, stream()>>>(p);

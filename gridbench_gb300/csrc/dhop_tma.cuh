@@ -194,10 +194,15 @@ __host__ __device__ inline unsigned tmaw_warp_bytes(int NSW, int LsE, int LsP, i
   return unsigned(STAGES) * unsigned(NSW) * blk + unsigned(NSW) * lb + ((unsigned(STAGES + 1) * 8u + 15u) & ~15u);
 }
 
-template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int STAGES, int MINB = 0>
-__global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1) k_dhop_tmaw(const DhopParams p) {
+template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int STAGES, int MINB = 0, int LSPC = 0>
+__global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1) k_dhop_tmaw(const DhopParams p_) {
   using T = typename Arith<PIN>::T;
   extern __shared__ __align__(128) unsigned char smem[];
+  DhopParams p = p_;
+  if constexpr (LSPC > 0) {
+    p.LsE = LSPC;
+    p.LsP = LSPC;
+  }
   const int LsE = p.LsE, LsP = p.LsP;
   const int Tps = LsE / N;
   const int NSW = 32 / Tps;
