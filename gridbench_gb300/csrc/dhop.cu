@@ -83,12 +83,12 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
   if (in->LsE % L.spt != 0) L.spt = 1;
   int NS = 0, tthreads = 0;
   size_t smem = 0;
-  const bool staged = L.mode == 1 || L.mode == 2 || L.mode == 4;
+  const bool staged = L.mode == 1 || L.mode == 2;
   if (staged && !tma_shape(in->prec, in->LsE, L, &NS, &tthreads, &smem)) L.mode = 0;
-  if (L.mode == 3 && (L.threads > 128 || L.spt != 2 || in->prec == GBDW_F64)) L.mode = 0;
+  if (L.mode == 3 && (in->prec != GBDW_F32 || L.spt != 2 || in->LsE != 16 || in->LsP != 16)) L.mode = 0;
+  if (L.mode == 3) L.threads = 64;
   const int64_t nthreads = p.nsite * (p.LsE / L.spt);
-  const int64_t blocks = (L.mode == 1 || L.mode == 2 || L.mode == 4) ? (p.nsite + NS - 1) / NS
-                                                                     : (nthreads + L.threads - 1) / L.threads;
+  const int64_t blocks = staged ? (p.nsite + NS - 1) / NS : (nthreads + L.threads - 1) / L.threads;
   Reduce red;
   if (norm2) {
     if (int st = reduce_scratch(blocks, 1, &red)) return st;
@@ -112,13 +112,7 @@ bool tma_shape(int prec, int LsE, DhopLaunch L, int* NS, int* threads, size_t* s
   const size_t esz = spinor_elem_bytes(prec);
   const size_t blk = 12 * size_t(padded_slices(prec, LsE)) * esz + (prec == GBDW_F16 ? 4 * size_t(LsE) : 0);
   const size_t lb = 8 * link_bytes(prec);
-  if (L.mode == 3) return false;  // direct form: no staging shape
-  if (L.mode == 4) {
-    if (L.threads > 128 || L.stages != 2) return false;
-    DhopLaunch L2 = L;
-    L2.mode = 2;
-    return tma_shape(prec, LsE, L2, NS, threads, smem);
-  }
+  if (L.mode == 3) return false;  // a direct form: no staging shape
   if (L.mode == 2) {
     // one ring per warp: a warp owns 32/Tps whole sites
     if (Tps > 32 || L.threads % 32 != 0 || L.threads > 256) return false;

@@ -531,12 +531,12 @@ __device__ __forceinline__ void dhop_thread(const DhopParams& p, unsigned site, 
 }
 
 // EPI 0: out = Dhop(in) ; EPI 1: out = M(in) (Shamir).  |out|^2 fused when p.partials != 0.
-// MINB > 0 caps registers so that MINB CTAs of up to 128 threads fit on an SM (more warps,
+// MINB > 0 caps registers so that MINB CTAs of up to MAXT threads fit on an SM (more warps,
 // more loads in flight); MINB = 0 leaves the compiler free up to 256 threads.
 // LSPC > 0: the launch guarantees LsE == LsP == LSPC, so every row offset is a compile-time
 // constant.
-template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int MINB = 0, int LSPC = 0>
-__global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1) k_dhop(const DhopParams p_) {
+template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int MINB = 0, int LSPC = 0, int MAXT = 128>
+__global__ void __launch_bounds__(MINB > 0 ? MAXT : 256, MINB > 0 ? MINB : 1) k_dhop(const DhopParams p_) {
   using T = typename Arith<PIN>::T;
   DhopParams p = p_;
   if constexpr (LSPC > 0) {
@@ -596,7 +596,7 @@ struct DhopLaunch {
   int threads;     // per CTA (target; the staged kernels round to whole sites)
   int spt;         // slices per thread
   int mode = 0;    // 0: direct loads, 1: TMA-staged (CTA ring), 2: TMA-staged (one ring per warp),
-                   // 3 / 4: forms 0 / 2 with registers capped for 5 CTAs of <= 128 threads per SM
+                   // 3: direct, FP32 Ls = 16 at compile time, registers balanced for 6 CTAs/SM
   int stages = 4;  // staged kernels: depth of the leg ring
 };
 

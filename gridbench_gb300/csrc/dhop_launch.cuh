@@ -6,18 +6,18 @@
 
 namespace gbdw {
 
-template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int MINB = 0>
+template <int PIN, int POUT, int GP, int DAG, int N, int EPI>
 int go_direct(const DhopParams& p, DhopLaunch L) {
   const int64_t nthreads = p.nsite * (p.LsE / N);
   const unsigned blocks = unsigned((nthreads + L.threads - 1) / L.threads);
-  if constexpr (PIN == GBDW_F32 && N == 2 && MINB == 0) {
+  if constexpr (PIN == GBDW_F32 && N == 2) {
     if (p.LsE == 16 && p.LsP == 16) {
       k_dhop<PIN, POUT, GP, DAG, N, EPI, 0, 16><<<blocks, L.threads, 0, stream()>>>(p);
       GBDW_LAUNCHED();
       return GBDW_OK;
     }
   }
-  k_dhop<PIN, POUT, GP, DAG, N, EPI, MINB><<<blocks, L.threads, 0, stream()>>>(p);
+  k_dhop<PIN, POUT, GP, DAG, N, EPI><<<blocks, L.threads, 0, stream()>>>(p);
   GBDW_LAUNCHED();
   return GBDW_OK;
 }
@@ -45,7 +45,7 @@ int go_tma(const DhopParams& p, DhopLaunch L) {
   return GBDW_OK;
 }
 
-template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int STAGES, int MINB = 0>
+template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int STAGES>
 int go_tmaw(const DhopParams& p, DhopLaunch L) {
   int NS = 0, threads = 0;
   size_t smem = 0;
@@ -53,9 +53,9 @@ int go_tmaw(const DhopParams& p, DhopLaunch L) {
     set_error("warp-staged hopping kernel: no admissible shape for this extent");
     return GBDW_ERR_INVALID;
   }
-  auto kern = (PIN == GBDW_F32 && N == 2 && MINB == 0 && STAGES == 2 && p.LsE == 16 && p.LsP == 16)
-                  ? k_dhop_tmaw<PIN, POUT, GP, DAG, N, EPI, STAGES, MINB, (PIN == GBDW_F32 && N == 2 && MINB == 0 && STAGES == 2) ? 16 : 0>
-                  : k_dhop_tmaw<PIN, POUT, GP, DAG, N, EPI, STAGES, MINB>;
+  auto kern = (PIN == GBDW_F32 && N == 2 && STAGES == 2 && p.LsE == 16 && p.LsP == 16)
+                  ? k_dhop_tmaw<PIN, POUT, GP, DAG, N, EPI, STAGES, (PIN == GBDW_F32 && N == 2 && STAGES == 2) ? 16 : 0>
+                  : k_dhop_tmaw<PIN, POUT, GP, DAG, N, EPI, STAGES>;
   static const void* opted_in[2] = {nullptr, nullptr};  // one attribute call per instance
   if (opted_in[0] != (const void*)kern && opted_in[1] != (const void*)kern) {
     cudaFuncAttributes fa;
@@ -77,9 +77,16 @@ int by_shape(const DhopParams& p, DhopLaunch L) {
     if (L.spt == S1) return L.stages == 2 ? go_tma<PIN, POUT, GP, DAG, S1, EPI, 2>(p, L) : go_tma<PIN, POUT, GP, DAG, S1, EPI, 4>(p, L);
     if (L.spt == S2) return L.stages == 2 ? go_tma<PIN, POUT, GP, DAG, S2, EPI, 2>(p, L) : go_tma<PIN, POUT, GP, DAG, S2, EPI, 4>(p, L);
   } else if (L.mode == 3) {
-    if (L.spt == 2 && PIN != GBDW_F64) return go_direct<PIN, POUT, GP, DAG, 2, EPI, 5>(p, L);
-  } else if (L.mode == 4) {
-    if (L.spt == 2 && PIN != GBDW_F64) return go_tmaw<PIN, POUT, GP, DAG, 2, EPI, 2, 5>(p, L);
+    // direct form, Ls = 16 rows at compile time, 64-thread CTAs, registers balanced for six
+    // CTAs per SM (the hoisted loads of the specialised kernel otherwise take ~250 registers)
+    if constexpr (PIN == GBDW_F32) {
+      if (L.spt == 2 && p.LsE == 16 && p.LsP == 16) {
+        const unsigned blocks = unsigned((p.nsite * 8 + 63) / 64);
+        k_dhop<PIN, POUT, GP, DAG, 2, EPI, 6, 16, 64><<<blocks, 64, 0, stream()>>>(p);
+        GBDW_LAUNCHED();
+        return GBDW_OK;
+      }
+    }
   } else if (L.mode == 2) {
     if (L.spt == S1) return L.stages == 2 ? go_tmaw<PIN, POUT, GP, DAG, S1, EPI, 2>(p, L) : go_tmaw<PIN, POUT, GP, DAG, S1, EPI, 4>(p, L);
     if (L.spt == S2) return L.stages == 2 ? go_tmaw<PIN, POUT, GP, DAG, S2, EPI, 2>(p, L) : go_tmaw<PIN, POUT, GP, DAG, S2, EPI, 4>(p, L);

@@ -194,8 +194,8 @@ __host__ __device__ inline unsigned tmaw_warp_bytes(int NSW, int LsE, int LsP, i
   return unsigned(STAGES) * unsigned(NSW) * blk + unsigned(NSW) * lb + ((unsigned(STAGES + 1) * 8u + 15u) & ~15u);
 }
 
-template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int STAGES, int MINB = 0, int LSPC = 0>
-__global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1) k_dhop_tmaw(const DhopParams p_) {
+template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int STAGES, int LSPC = 0>
+__global__ void __launch_bounds__(256) k_dhop_tmaw(const DhopParams p_) {
   using T = typename Arith<PIN>::T;
   extern __shared__ __align__(128) unsigned char smem[];
   DhopParams p = p_;

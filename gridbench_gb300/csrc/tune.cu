@@ -66,16 +66,16 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
       if (in->LsE % spt != 0 || (in->prec == GBDW_F64 && spt > 2)) continue;
       cands.push_back(DhopLaunch{th, spt, 0, 4});
     }
-    for (int mode : {1, 2, 4})
+    for (int mode : {1, 2})
       for (int spt : {s1, s2})
         for (int stages : {2, 4}) {
           DhopLaunch L{th, spt, mode, stages};
           int ns, tt;
           size_t sm;
-          if ((mode != 4 || spt == 2) && tma_shape(in->prec, in->LsE, L, &ns, &tt, &sm)) cands.push_back(L);
+          if (tma_shape(in->prec, in->LsE, L, &ns, &tt, &sm)) cands.push_back(L);
         }
-    if (th <= 128 && in->prec != GBDW_F64 && in->LsE % 2 == 0) cands.push_back(DhopLaunch{th, 2, 3, 4});
   }
+  if (in->prec == GBDW_F32 && in->LsE == 16 && in->LsP == 16) cands.push_back(DhopLaunch{64, 2, 3, 4});
   cudaEvent_t a, b;
   GBDW_CUDA(cudaEventCreate(&a));
   GBDW_CUDA(cudaEventCreate(&b));
@@ -120,18 +120,18 @@ int gbdw_tune_query(const gbdw_gauge* g, const gbdw_field* in, int cfg[2]) {
 
 int gbdw_tune_set(const gbdw_gauge* g, const gbdw_field* in, int threads, int spt, int form, int stages) {
   if (!g || !in || threads < 32 || threads > 256 || threads % 32 != 0 || !(spt == 1 || spt == 2 || spt == 4) ||
-      in->LsE % spt != 0 || (in->prec == GBDW_F64 && spt > 2) || form < 0 || form > 4 ||
+      in->LsE % spt != 0 || (in->prec == GBDW_F64 && spt > 2) || form < 0 || form > 3 ||
       (stages != 2 && stages != 4)) {
     set_error("gbdw_tune_set: threads 32..256 in steps of 32, spt 1/2/4 dividing Ls*nrhs (<= 2 for F64), "
               "form 0/1/2, stages 2/4");
     return GBDW_ERR_INVALID;
   }
   const DhopLaunch L{threads, spt, form, stages};
-  if (form == 3 && (threads > 128 || spt != 2 || in->prec == GBDW_F64)) {
-    set_error("gbdw_tune_set: form 3 takes 2 slices per thread, <= 128 threads, F32/F16");
+  if (form == 3 && (spt != 2 || in->prec != GBDW_F32 || in->LsE != 16 || in->LsP != 16)) {
+    set_error("gbdw_tune_set: form 3 is the FP32 Ls*nrhs = 16 kernel with 2 slices per thread");
     return GBDW_ERR_INVALID;
   }
-  if (form == 1 || form == 2 || form == 4) {
+  if (form == 1 || form == 2) {
     const int s1 = in->prec == GBDW_F16 ? 2 : 1, s2 = in->prec == GBDW_F16 ? 4 : 2;
     int ns, tt;
     size_t sm;
@@ -189,7 +189,7 @@ int gbdw_tune_load(const char* path) {
     if (lb == std::string::npos) break;
     if (sscanf(key.c_str(), "g%d_s%d_L%d_e%d", &gp, &sp, &LsE, &epi) == 4 &&
         sscanf(text.c_str() + lb, "[%d , %d , %d , %d]", &th, &spt, &mode, &stages) >= 2 && th > 0 && th <= 256 &&
-        th % 32 == 0 && (spt == 1 || spt == 2 || spt == 4) && mode >= 0 && mode <= 4 && (stages == 2 || stages == 4)) {
+        th % 32 == 0 && (spt == 1 || spt == 2 || spt == 4) && mode >= 0 && mode <= 3 && (stages == 2 || stages == 4)) {
       set_tuned_launch(gp, sp, LsE, epi, DhopLaunch{th, spt, mode, stages});
       ++loaded;
     }

@@ -151,6 +151,28 @@ def test_every_launch_shape(gpu, prec, threads, Ls):
     gb.synchronize()
 
 
+@pytest.mark.parametrize("shape", [(128, 2, 0, 4), (64, 2, 3, 4), (128, 2, 2, 2), (64, 2, 2, 2)])
+def test_fp32_ls16_specialised_kernels(gpu, shape):
+    """FP32 with Ls*nrhs = 16 runs kernels whose row stride is a compile-time constant (the
+    direct form, form 3 and the two-stage warp rings): Dhop, DhopDag and the fused M."""
+    c = make_case((4, 6, 2, 3), 16)
+    lat = gb.Lattice.from_table(c["nbr"], c["prm"], c["nsite"], 16)
+    g = gb.Gauge(lat, c["U"], gb.F32)
+    x = gb.Field(lat, gb.F32).load(c["phi"])
+    y = gb.Field(lat, gb.F32)
+    gb.tune_set(g, x, *shape)
+    assert tuple(gb.tune_query(g, x)) == shape
+    for dag in (0, 1):
+        ref = oracle.dslash(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], 16, dag)
+        y.zero()
+        gb.dhop(g, y, x, dag)
+        assert rel_err(y.numpy(), ref) < TOL[gb.F32], (shape, dag)
+        refm = oracle.dwf_m(c["U"], c["phi"], c["nbr"], c["nsite"], 16, 1.8, 0.01, dag)
+        gb.dwf_m(g, y, x, 1.8, 0.01, dag)
+        assert rel_err(y.numpy(), refm) < TOL[gb.F32], (shape, dag)
+    gb.synchronize()
+
+
 def test_periodic_lattice_equals_table_lattice(gpu):
     c = make_case((4, 6, 2, 4), 4)
     ref = oracle.dslash(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], 4)
