@@ -506,7 +506,8 @@ ONLY = {  # name -> (dims, Ls, spinor precision, gauge precision, dag)
 
 def run_only(args) -> dict:
     """One hopping-term workload, nothing else: the command profiles are captured with.
-    --shape threads,slices,form,stages pins the launch shape (form 0 direct, 1 TMA-staged);
+    --shape threads,slices,form,stages pins the launch shape (form 0 direct, 1 TMA-staged CTA
+    ring, 2 TMA-staged warp rings, 3 direct FP32 Ls=16);
     without it the autotuner picks."""
     import gridbench_gb300 as gb
     dims, Ls, sp, gp, dag = ONLY[args.only]
