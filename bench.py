@@ -435,7 +435,7 @@ def run_ours(args, D: Dist) -> dict | None:
                    "l2": "inputs larger than L2: two alternating in/out pairs, 476 MB vs 129 MB L2",
                    "launch": {"threads": cfg[0], "slices_per_thread": cfg[1],
                               "form": {0: "direct", 1: "tma-staged (CTA ring)", 2: "tma-staged (warp rings)",
-                                       3: "direct (FP32 Ls=16 specialised)"}[cfg[2]],
+                                       3: "direct (Ls=16 specialised)"}[cfg[2]],
                               "stages": cfg[3]}},
         "rel_err_vs_fp64": rel,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
@@ -507,7 +507,7 @@ ONLY = {  # name -> (dims, Ls, spinor precision, gauge precision, dag)
 def run_only(args) -> dict:
     """One hopping-term workload, nothing else: the command profiles are captured with.
     --shape threads,slices,form,stages pins the launch shape (form 0 direct, 1 TMA-staged CTA
-    ring, 2 TMA-staged warp rings, 3 direct FP32 Ls=16);
+    ring, 2 TMA-staged warp rings, 3 direct specialised for Ls=16);
     without it the autotuner picks."""
     import gridbench_gb300 as gb
     dims, Ls, sp, gp, dag = ONLY[args.only]

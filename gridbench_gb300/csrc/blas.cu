@@ -150,11 +150,10 @@ __global__ void k_xmy_norm(FieldRef b, FieldRef t, FieldOut r, int64_t nsite, in
   grid_sum<1>(acc, red.partials, red.counter, red.result);
 }
 
-// x += alpha p ; r -= alpha Ap ; |r|^2
-template <int PX, int PP, int PR, int PA>
-__global__ void k_cg_xr(double alpha, FieldOut x, FieldRef p, FieldOut r, FieldRef ap, int64_t nsite, int LsE,
-                        Reduce red) {
-  using T = typename Calc<(PX == GBDW_F64 || PR == GBDW_F64) ? GBDW_F64 : GBDW_F32>::T;
+// r -= alpha Ap ; |r|^2
+template <int PR, int PA>
+__global__ void k_cg_r(double alpha, FieldOut r, FieldRef ap, int64_t nsite, int LsE, Reduce red) {
+  using T = typename Calc<PR>::T;
   double acc[1] = {0.0};
   const int64_t n = nsite * LsE;
   const T al = T(alpha);
@@ -162,11 +161,6 @@ __global__ void k_cg_xr(double alpha, FieldOut x, FieldRef p, FieldOut r, FieldR
     const int64_t site = i / LsE;
     const int e = int(i - site * LsE);
     T u[24], v[24];
-    ld24<PX>(x.d, x.n, site, e, LsE, x.LsP, u);
-    ld24<PP>(p.d, p.n, site, e, LsE, p.LsP, v);
-#pragma unroll
-    for (int k = 0; k < 24; ++k) u[k] += al * v[k];
-    st24<PX>(x.d, x.n, site, e, LsE, x.LsP, u);
     ld24<PR>(r.d, r.n, site, e, LsE, r.LsP, u);
     ld24<PA>(ap.d, ap.n, site, e, LsE, ap.LsP, v);
 #pragma unroll
@@ -174,6 +168,30 @@ __global__ void k_cg_xr(double alpha, FieldOut x, FieldRef p, FieldOut r, FieldR
     acc[0] += double(st24<PR>(r.d, r.n, site, e, LsE, r.LsP, u));
   }
   grid_sum<1>(acc, red.partials, red.counter, red.result);
+}
+
+// x += alpha p ; p = r + beta p (both with the old p) ; optionally q = p
+template <int PX, int PP, int PR, int PQ>
+__global__ void k_cg_xp(double alpha, double beta, FieldOut x, FieldOut p, FieldRef r, FieldOut q, int64_t nsite,
+                        int LsE) {
+  using T = typename Calc<(PX == GBDW_F64 || PR == GBDW_F64) ? GBDW_F64 : GBDW_F32>::T;
+  const int64_t n = nsite * LsE;
+  const T al = T(alpha), be = T(beta);
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t site = i / LsE;
+    const int e = int(i - site * LsE);
+    T u[24], v[24];
+    ld24<PP>(p.d, p.n, site, e, LsE, p.LsP, v);
+    ld24<PX>(x.d, x.n, site, e, LsE, x.LsP, u);
+#pragma unroll
+    for (int k = 0; k < 24; ++k) u[k] += al * v[k];
+    st24<PX>(x.d, x.n, site, e, LsE, x.LsP, u);
+    ld24<PR>(r.d, r.n, site, e, LsE, r.LsP, u);
+#pragma unroll
+    for (int k = 0; k < 24; ++k) v[k] = u[k] + be * v[k];
+    st24<PP>(p.d, p.n, site, e, LsE, p.LsP, v);
+    if (PQ >= 0) st24<PQ < 0 ? GBDW_F32 : PQ>(q.d, q.n, site, e, LsE, q.LsP, v);
+  }
 }
 
 // p = r + beta p ; optionally q = p (a lower-precision copy that feeds the operator)
@@ -245,29 +263,54 @@ int blas_xmy_norm(const gbdw_field* b, const gbdw_field* t, gbdw_field* r, doubl
   return reduce_fetch(red, 1, rr);
 }
 
-int blas_cg_xr(double alpha, gbdw_field* x, const gbdw_field* p, gbdw_field* r, const gbdw_field* ap, double* rr) {
+int blas_cg_r(double alpha, gbdw_field* r, const gbdw_field* ap, double* rr) {
   const int64_t g = grid_for(r);
   Reduce red;
   if (int st = reduce_scratch(g, 1, &red)) return st;
   const int64_t ns = r->lat->nsite;
   const int L = r->LsE;
-  const int key = ((x->prec * 4 + p->prec) * 4 + r->prec) * 4 + ap->prec;
-#define GBDW_XR(PX, PP, PR, PA)                                                                          \
-  case ((PX * 4 + PP) * 4 + PR) * 4 + PA:                                                                \
-    k_cg_xr<PX, PP, PR, PA><<<unsigned(g), kThreads, 0, stream()>>>(alpha, out(x), ref(p), out(r), ref(ap), ns, L, red); \
+  const int key = r->prec * 4 + ap->prec;
+#define GBDW_R(PR, PA)                                                                                  \
+  case PR * 4 + PA:                                                                                     \
+    k_cg_r<PR, PA><<<unsigned(g), kThreads, 0, stream()>>>(alpha, out(r), ref(ap), ns, L, red);         \
     break;
   switch (key) {
-    GBDW_XR(GBDW_F64, GBDW_F64, GBDW_F64, GBDW_F64)  // FP64 solve
-    GBDW_XR(GBDW_F64, GBDW_F64, GBDW_F64, GBDW_F32)  // plain: FP64 vectors, FP32 operator
-    GBDW_XR(GBDW_F32, GBDW_F16, GBDW_F32, GBDW_F16)  // mixed, FP16 sloppy
-    GBDW_XR(GBDW_F32, GBDW_F32, GBDW_F32, GBDW_F32)  // mixed, FP32 sloppy
+    GBDW_R(GBDW_F64, GBDW_F64)  // FP64 solve
+    GBDW_R(GBDW_F64, GBDW_F32)  // plain: FP64 vectors, FP32 operator
+    GBDW_R(GBDW_F32, GBDW_F16)  // mixed, FP16 sloppy
+    GBDW_R(GBDW_F32, GBDW_F32)  // mixed, FP32 sloppy
     default:
-      set_error("blas_cg_xr: unsupported precision combination");
+      set_error("blas_cg_r: unsupported precision combination");
       return GBDW_ERR_INVALID;
   }
-#undef GBDW_XR
+#undef GBDW_R
   GBDW_LAUNCHED();
   return reduce_fetch(red, 1, rr);
+}
+
+int blas_cg_xp(double alpha, double beta, gbdw_field* x, gbdw_field* p, const gbdw_field* r, gbdw_field* q) {
+  const int64_t g = grid_for(r);
+  const int64_t ns = r->lat->nsite;
+  const int L = r->LsE;
+  const int qp = q ? q->prec : -1;
+  FieldOut qo = q ? out(q) : FieldOut{nullptr, nullptr, 0};
+  const int key = ((x->prec * 4 + p->prec) * 4 + r->prec) * 8 + (qp + 1);
+#define GBDW_XP(PX, PP, PR, PQ)                                                                              \
+  case ((PX * 4 + PP) * 4 + PR) * 8 + (PQ + 1):                                                              \
+    k_cg_xp<PX, PP, PR, PQ><<<unsigned(g), kThreads, 0, stream()>>>(alpha, beta, out(x), out(p), ref(r), qo, ns, L); \
+    break;
+  switch (key) {
+    GBDW_XP(GBDW_F64, GBDW_F64, GBDW_F64, -1)
+    GBDW_XP(GBDW_F64, GBDW_F64, GBDW_F64, GBDW_F32)
+    GBDW_XP(GBDW_F32, GBDW_F16, GBDW_F32, -1)
+    GBDW_XP(GBDW_F32, GBDW_F32, GBDW_F32, -1)
+    default:
+      set_error("blas_cg_xp: unsupported precision combination");
+      return GBDW_ERR_INVALID;
+  }
+#undef GBDW_XP
+  GBDW_LAUNCHED();
+  return GBDW_OK;
 }
 
 int blas_cg_p(double beta, const gbdw_field* r, gbdw_field* p, gbdw_field* q) {

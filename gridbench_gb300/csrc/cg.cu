@@ -144,14 +144,24 @@ extern "C" int gbdw_cg_solve(const gbdw_gauge* g64, const gbdw_gauge* g32, const
     }
     const double alpha = rr / pap;
     double rr_new = 0.0;
-    TRY(blas_cg_xr(alpha, xs, p, rs, ap, &rr_new));
+    TRY(blas_cg_r(alpha, rs, ap, &rr_new));
     ++it;
     if (!std::isfinite(rr_new)) {
+      TRY(blas_axpby(alpha, p, 1.0, xs));
       set_error("gbdw_cg_solve: residual became non-finite");
       err = GBDW_ERR_DIVERGED;
       break;
     }
-    if (rr_new < delta * delta * maxrr || rr_new <= stop) {
+    if (!(rr_new < delta * delta * maxrr || rr_new <= stop)) {
+      // the common iteration: x and p updated in one pass over the vectors
+      const double beta = rr_new / rr;
+      TRY(blas_cg_xp(alpha, beta, xs, p, rs, pq));
+      rr = rr_new;
+      if (rr > maxrr) maxrr = rr;
+      continue;
+    }
+    TRY(blas_axpby(alpha, p, 1.0, xs));
+    {
       // reliable update
       if (mode == GBDW_CG_MIXED) {
         TRY(blas_axpby(1.0, xs, 1.0, x));

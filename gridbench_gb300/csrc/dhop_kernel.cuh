@@ -596,7 +596,7 @@ struct DhopLaunch {
   int threads;     // per CTA (target; the staged kernels round to whole sites)
   int spt;         // slices per thread
   int mode = 0;    // 0: direct loads, 1: TMA-staged (CTA ring), 2: TMA-staged (one ring per warp),
-                   // 3: direct, FP32 Ls = 16 at compile time, registers balanced for 6 CTAs/SM
+                   // 3: direct, FP32/FP16 Ls = 16 at compile time, registers balanced for 6 CTAs/SM
   int stages = 4;  // staged kernels: depth of the leg ring
 };
 

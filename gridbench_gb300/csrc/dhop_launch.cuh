@@ -79,7 +79,7 @@ int by_shape(const DhopParams& p, DhopLaunch L) {
   } else if (L.mode == 3) {
     // direct form, Ls = 16 rows at compile time, 64-thread CTAs, registers balanced for six
     // CTAs per SM (the hoisted loads of the specialised kernel otherwise take ~250 registers)
-    if constexpr (PIN == GBDW_F32) {
+    if constexpr (PIN == GBDW_F32 || PIN == GBDW_F16) {
       if (L.spt == 2 && p.LsE == 16 && p.LsP == 16) {
         const unsigned blocks = unsigned((p.nsite * 8 + 63) / 64);
         k_dhop<PIN, POUT, GP, DAG, 2, EPI, 6, 16, 64><<<blocks, 64, 0, stream()>>>(p);

@@ -1,7 +1,8 @@
-// Autotuner for the hopping kernel: times every admissible (threads per CTA, slices per
-// thread) pair on the caller's own fields with CUDA events and keeps the fastest, keyed by
-// (gauge precision, spinor precision, innermost extent Ls*nrhs, epilogue).  The cache can be
-// written to and read back from a small JSON object {"key": [threads, slices], ...}.
+// Autotuner for the hopping kernel: times every admissible launch shape (threads per CTA,
+// slices per thread, form, ring stages) on the caller's own fields with CUDA events and keeps
+// the fastest, keyed by (gauge precision, spinor precision, innermost extent Ls*nrhs,
+// epilogue).  The cache can be written to and read back from a small JSON object
+// {"key": [threads, slices, form, stages], ...}.
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -75,7 +76,7 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
           if (tma_shape(in->prec, in->LsE, L, &ns, &tt, &sm)) cands.push_back(L);
         }
   }
-  if (in->prec == GBDW_F32 && in->LsE == 16 && in->LsP == 16) cands.push_back(DhopLaunch{64, 2, 3, 4});
+  if (in->prec != GBDW_F64 && in->LsE == 16 && in->LsP == 16) cands.push_back(DhopLaunch{64, 2, 3, 4});
   cudaEvent_t a, b;
   GBDW_CUDA(cudaEventCreate(&a));
   GBDW_CUDA(cudaEventCreate(&b));
@@ -108,7 +109,7 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
   return status;
 }
 
-int gbdw_tune_query(const gbdw_gauge* g, const gbdw_field* in, int cfg[2]) {
+int gbdw_tune_query(const gbdw_gauge* g, const gbdw_field* in, int cfg[4]) {
   if (!g || !in || !cfg) return GBDW_ERR_INVALID;
   const DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, 0);
   cfg[0] = L.threads;
@@ -123,12 +124,12 @@ int gbdw_tune_set(const gbdw_gauge* g, const gbdw_field* in, int threads, int sp
       in->LsE % spt != 0 || (in->prec == GBDW_F64 && spt > 2) || form < 0 || form > 3 ||
       (stages != 2 && stages != 4)) {
     set_error("gbdw_tune_set: threads 32..256 in steps of 32, spt 1/2/4 dividing Ls*nrhs (<= 2 for F64), "
-              "form 0/1/2, stages 2/4");
+              "form 0..3, stages 2/4");
     return GBDW_ERR_INVALID;
   }
   const DhopLaunch L{threads, spt, form, stages};
-  if (form == 3 && (spt != 2 || in->prec != GBDW_F32 || in->LsE != 16 || in->LsP != 16)) {
-    set_error("gbdw_tune_set: form 3 is the FP32 Ls*nrhs = 16 kernel with 2 slices per thread");
+  if (form == 3 && (spt != 2 || in->prec == GBDW_F64 || in->LsE != 16 || in->LsP != 16)) {
+    set_error("gbdw_tune_set: form 3 is the FP32/FP16 Ls*nrhs = 16 kernel with 2 slices per thread");
     return GBDW_ERR_INVALID;
   }
   if (form == 1 || form == 2) {
@@ -177,7 +178,7 @@ int gbdw_tune_load(const char* path) {
   size_t n;
   while ((n = fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, n);
   fclose(f);
-  // Entries look like "g1_s1_L16_e0": [128, 2]
+  // Entries look like "g1_s1_L16_e0": [128, 2, 0, 4] (older two-number entries keep form 0)
   size_t pos = 0;
   int loaded = 0;
   while ((pos = text.find('"', pos)) != std::string::npos) {

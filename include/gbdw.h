@@ -197,7 +197,7 @@ int gbdw_tune_load(const char* path);
 int gbdw_tune_save(const char* path);
 /* Writes the chosen shape for a field into cfg[4]: threads per CTA, slices per thread,
  * form (0 direct loads, 1 TMA-staged neighbour blocks with one ring per CTA, 2 the same with
- * one ring per warp, 3 the direct form specialised for FP32 with Ls*nrhs = 16) and stages of
+ * one ring per warp, 3 the direct form specialised for FP32/FP16 with Ls*nrhs = 16) and stages of
  * the staged forms. */
 int gbdw_tune_query(const gbdw_gauge* g, const gbdw_field* in, int cfg[4]);
 /* Pins the shape for fields like `in` (threads a multiple of 32 up to 256; slices per thread

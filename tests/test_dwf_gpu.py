@@ -111,3 +111,24 @@ def test_m_rejects_multi_rhs_and_inplace(gpu):
         gb.dwf_m(g, Y, X, M5, MF)
     with pytest.raises(gb.GbdwError):
         gb.dhop(g, x, x)
+
+
+@pytest.mark.parametrize("gprec", [gb.F16, gb.BF16])
+def test_fp16_ls16_specialised_form(gpu, gprec):
+    """Form 3 (row stride fixed at Ls = 16 at compile time) on FP16 spinors: Dhop, DhopDag,
+    M and M^dagger with the fused norm."""
+    c, lat, g, x = _setup((4, 2, 6, 2), 16, gb.F16, gprec)
+    y = gb.Field(lat, gb.F16)
+    gb.tune_set(g, x, 64, 2, 3, 4)
+    assert tuple(gb.tune_query(g, x)) == (64, 2, 3, 4)
+    tol = 5e-3 if gprec == gb.F16 else 3e-2
+    for dag in (0, 1):
+        n2 = gb.dwf_m(g, y, x, M5, MF, dag, want_norm=True)
+        ref = oracle.dwf_m(c["U"], c["phi"], c["nbr"], c["nsite"], 16, M5, MF, dag)
+        out = y.numpy()
+        assert rel_err(out, ref) < tol
+        assert abs(n2 - float(np.sum(out ** 2))) / n2 < 1e-5
+        gb.dhop(g, y, x, dag)
+        ref = oracle.dslash(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], 16, dag)
+        assert rel_err(y.numpy(), ref) < tol
+    gb.synchronize()
