@@ -128,6 +128,15 @@ class Lattice(_Handle):
         check(load().gbdw_lattice_info(self.h, a))
         return {"sites": a[0], "Ls": a[1], "nsimd": a[2], "fast": bool(a[3])}
 
+    def checkerboard(self) -> tuple:
+        """(even, odd) half lattices of this periodic lattice (every extent even); half-site
+        index = parent site // 2."""
+        e, o = Lattice(), Lattice()
+        check(load().gbdw_lattice_checkerboard(self.h, C.byref(e.h), C.byref(o.h)))
+        e.parent = o.parent = self
+        e.parity, o.parity = 0, 1
+        return e, o
+
 
 class Gauge(_Handle):
     _destroy = "gbdw_gauge_destroy"
@@ -144,6 +153,14 @@ class Gauge(_Handle):
         U = np.ascontiguousarray(U)
         src = F64 if U.dtype == np.float64 else F32
         check(load().gbdw_gauge_create(C.byref(self.h), lat.h, prec, _ptr(U), src))
+
+    def checkerboard(self, half: Lattice) -> "Gauge":
+        """The links of one half lattice's sites (same precision), for the even-odd operators."""
+        g = Gauge.__new__(Gauge)
+        _Handle.__init__(g)
+        g.lat, g.prec, g.parent = half, self.prec, self
+        check(load().gbdw_gauge_checkerboard(C.byref(g.h), self.h, half.h))
+        return g
 
 
 class Field(_Handle):
@@ -198,6 +215,16 @@ class Field(_Handle):
         """self = a x + b self"""
         check(load().gbdw_axpby(a, x.h, b, self.h))
 
+    def pick(self, full: "Field") -> "Field":
+        """self (a half-lattice field) <- the sites of its parity from full"""
+        check(load().gbdw_field_pick(self.h, full.h))
+        return self
+
+    def place_into(self, full: "Field") -> "Field":
+        """full <- self on self's parity (the other parity of full is kept)"""
+        check(load().gbdw_field_place(full.h, self.h))
+        return full
+
 
 def dhop(g: Gauge, out: Field, inp: Field, dag: int = 0) -> None:
     check(load().gbdw_dhop(g.h, out.h, inp.h, int(dag)))
@@ -213,6 +240,52 @@ def dwf_mdagm(g: Gauge, out: Field, tmp: Field, inp: Field, M5: float, mf: float
     v = C.c_double()
     check(load().gbdw_dwf_mdagm(g.h, out.h, tmp.h, inp.h, M5, mf, C.byref(v)))
     return v.value
+
+
+def dhop_eo(g: Gauge, out: Field, inp: Field, dag: int = 0) -> None:
+    """out (g's half lattice) = Dhop from the partner half's inp"""
+    check(load().gbdw_dhop_eo(g.h, out.h, inp.h, int(dag)))
+
+
+def dwf_meo(g: Gauge, out: Field, inp: Field, cen: Field, M5: float, mf: float, dag: int = 0,
+            khop: float = 0.5) -> None:
+    """out = D5 cen - khop Dhop inp on g's half lattice (khop 1/2: M's rows of that parity)"""
+    check(load().gbdw_dwf_meo(g.h, out.h, inp.h, cen.h, M5, mf, int(dag), khop))
+
+
+def dwf_m5inv(out: Field, inp: Field, M5: float, mf: float, dag: int = 0) -> None:
+    check(load().gbdw_dwf_m5inv(out.h, inp.h, M5, mf, int(dag)))
+
+
+def dwf_mpc(gp: Gauge, gq: Gauge, out: Field, tq1: Field, tq2: Field, inp: Field, M5: float, mf: float,
+            dag: int = 0, want_norm: bool = False):
+    v = C.c_double()
+    check(load().gbdw_dwf_mpc(gp.h, gq.h, out.h, tq1.h, tq2.h, inp.h, M5, mf, int(dag),
+                              C.byref(v) if want_norm else None))
+    return v.value if want_norm else None
+
+
+def dwf_mpcdagmpc(gp: Gauge, gq: Gauge, out: Field, tp: Field, tq1: Field, tq2: Field, inp: Field, M5: float,
+                  mf: float) -> float:
+    v = C.c_double()
+    check(load().gbdw_dwf_mpcdagmpc(gp.h, gq.h, out.h, tp.h, tq1.h, tq2.h, inp.h, M5, mf, C.byref(v)))
+    return v.value
+
+
+def cg_solve_eo(g64: Sequence[Gauge], x: Field, b: Field, M5: float, mf: float, mode: int, tol: float = 1e-10,
+                max_iter: int = 20000, delta: float = 0.1, g32: Sequence[Gauge] | None = None,
+                gsloppy: Sequence[Gauge] | None = None, sloppy_prec: int = F16) -> dict:
+    """M x = b by CG on the odd Schur normal system; g64/g32/gsloppy are (even, odd) gauge
+    halves.  true_residual is the full system's |b - M x| / |b|."""
+    def pair(gs):
+        return (C.c_void_p * 2)(gs[0].h.value, gs[1].h.value) if gs is not None else None
+    prm = CGParams(tol, max_iter, delta, sloppy_prec, gsloppy[0].prec if gsloppy is not None else F16)
+    st = CGStats()
+    status = load().gbdw_cg_solve_eo(pair(g64), pair(g32), pair(gsloppy), x.h, b.h, M5, mf, mode, C.byref(prm),
+                                     C.byref(st))
+    check(status)
+    return {"iterations": st.iterations, "reliable_updates": st.reliable_updates,
+            "true_residual": st.true_residual, "seconds": st.seconds, "final_rr": st.final_rr}
 
 
 def cg_solve(g64: Gauge, x: Field, b: Field, M5: float, mf: float, mode: int, tol: float = 1e-10,

@@ -78,6 +78,16 @@ PROTOTYPES = {
     "gbdw_dot": (_i, [_vp, _vp, _dp, _dp]),
     "gbdw_axpby": (_i, [_d, _vp, _d, _vp]),
     "gbdw_cg_solve": (_i, [_vp, _vp, _vp, _vp, _vp, _d, _d, _i, C.POINTER(CGParams), C.POINTER(CGStats)]),
+    "gbdw_lattice_checkerboard": (_i, [_vp, _pp, _pp]),
+    "gbdw_gauge_checkerboard": (_i, [_pp, _vp, _vp]),
+    "gbdw_field_pick": (_i, [_vp, _vp]),
+    "gbdw_field_place": (_i, [_vp, _vp]),
+    "gbdw_dhop_eo": (_i, [_vp, _vp, _vp, _i]),
+    "gbdw_dwf_meo": (_i, [_vp, _vp, _vp, _vp, _d, _d, _i, _d]),
+    "gbdw_dwf_m5inv": (_i, [_vp, _vp, _d, _d, _i]),
+    "gbdw_dwf_mpc": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _d, _d, _i, _dp]),
+    "gbdw_dwf_mpcdagmpc": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, _d, _dp]),
+    "gbdw_cg_solve_eo": (_i, [_pp, _pp, _pp, _vp, _vp, _d, _d, _i, C.POINTER(CGParams), C.POINTER(CGStats)]),
     "gbdw_batch_create": (_i, [_pp, _i, _pp, _pp, _pp, _i]),
     "gbdw_batch_run": (_i, [_vp]),
     "gbdw_batch_destroy": (_i, [_vp]),

@@ -55,6 +55,13 @@ struct gbdw_lattice {
   bool fast;         // 4D factorised table available
   uint32_t* nbr4;    // [nsite][8] (fast)
   uint32_t* nbr5;    // [nsite][Ls][8] neighbour (site*Ls+s) in device numbering (general)
+  // Checkerboarded half lattice (even-odd): the sites of one 4D parity of a periodic parent,
+  // numbered site = parent_site / 2.  nbr4 then holds neighbour indices into the partner
+  // half (the other parity), and cbsite[site] the parent site.
+  int parity = -1;                         // -1: not a half lattice
+  const gbdw_lattice* parent = nullptr;
+  const gbdw_lattice* partner = nullptr;   // the other parity of the same parent
+  uint32_t* cbsite = nullptr;              // [nsite] parent site index
 };
 
 struct gbdw_gauge {

@@ -63,11 +63,16 @@ DhopParams make_params(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* i
 }
 
 int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag, int epi, double a5, double mf,
-             double* norm2, bool fetch) {
+             double* norm2, bool fetch, const gbdw_field* cen, double khop) {
   if (int st = ensure_device()) return st;
   DhopParams p = make_params(g, out, in);
   p.a5 = a5;
   p.mf = mf;
+  p.khop = khop;
+  if (cen) {
+    p.cen = cen->d;
+    p.cen_norm = cen->norm;
+  }
   if (!g->lat->fast) {
     if (epi || norm2 || in->nrhs != 1) {
       set_error("general (non-factorisable) tables support the plain hopping term only");

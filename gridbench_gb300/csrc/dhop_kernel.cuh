@@ -381,6 +381,11 @@ struct DhopParams {
   unsigned* counter;
   double* result;
   unsigned* err;         // device error word (bounded waits that expired)
+  // M epilogue: the field of the diagonal (5th-dimension) part, when it is not `in` (the
+  // even-odd Schur operator), and the coefficient of the hopping term (1/2 for M).
+  const void* cen = nullptr;
+  const float* cen_norm = nullptr;
+  double khop = 0.5;
 };
 
 // Writes N slices of v[N][12] (slices e0.., norms for F16); returns the sum of squares of
@@ -446,20 +451,23 @@ __device__ __forceinline__ double sumsq(const cpx<float> (&)[N][12]) {
 }
 
 // ------------------------------------------------------------------ Shamir 5D terms
-// out(s) = a5 psi(s) - 1/2 D(s) - [P- psi(s+1) + P+ psi(s-1)]       (dag = 0)
-// out(s) = a5 psi(s) - 1/2 D(s) - [P+ psi(s+1) + P- psi(s-1)]       (dag = 1)
+// out(s) = a5 psi(s) - k D(s) - [P- psi(s+1) + P+ psi(s-1)]       (dag = 0)
+// out(s) = a5 psi(s) - k D(s) - [P+ psi(s+1) + P- psi(s-1)]       (dag = 1)
 // P+ keeps spins 0,1 and P- spins 2,3 (gamma5 = diag(1,1,-1,-1)); a step across the
-// s boundary picks up -mf.  Requires nrhs == 1 (LsE == Ls).
+// s boundary picks up -mf.  k = p.khop (1/2 for M) and psi is p.cen when set, else the
+// hopping input.  Requires nrhs == 1 (LsE == Ls).
 template <int PIN, int DAG, int N, class T>
 __device__ __forceinline__ void dwf_epilogue(const DhopParams& p, int64_t site, int s0, cpx<T> (&acc)[N][12]) {
   const int Ls = p.Ls;
   const int LsP = p.LsP;
   const int64_t row0 = site * 12;
+  const void* cin = p.cen ? p.cen : p.in;
+  const float* cnorm = p.cen ? p.cen_norm : p.in_norm;
   cpx<T> cen[N][12];
 #pragma unroll
   for (int k = 0; k < 12; ++k) {
     cpx<T> x[N];
-    Vec<PIN, N>::load(p.in, row0 + k, s0, LsP, x);
+    Vec<PIN, N>::load(cin, row0 + k, s0, LsP, x);
 #pragma unroll
     for (int j = 0; j < N; ++j) cen[j][k] = x[j];
   }
@@ -472,13 +480,13 @@ __device__ __forceinline__ void dwf_epilogue(const DhopParams& p, int64_t site, 
   cpx<T> lo[6], hi[6];
 #pragma unroll
   for (int k = 0; k < 6; ++k) {
-    lo[k] = Elem<PIN>::ld(p.in, row0 + LO0 * 3 + k, slo, LsP);
-    hi[k] = Elem<PIN>::ld(p.in, row0 + HI0 * 3 + k, shi, LsP);
+    lo[k] = Elem<PIN>::ld(cin, row0 + LO0 * 3 + k, slo, LsP);
+    hi[k] = Elem<PIN>::ld(cin, row0 + HI0 * 3 + k, shi, LsP);
   }
   T nlo = flo, nhi = fhi;
   if constexpr (PIN == GBDW_F16) {
     float nc[N];
-    load_norms<N>(p.in_norm, site * Ls + s0, nc);
+    load_norms<N>(cnorm, site * Ls + s0, nc);
 #pragma unroll
     for (int j = 0; j < N; ++j)
 #pragma unroll
@@ -486,16 +494,16 @@ __device__ __forceinline__ void dwf_epilogue(const DhopParams& p, int64_t site, 
         cen[j][k].r *= nc[j];
         cen[j][k].i *= nc[j];
       }
-    nlo *= __ldg(p.in_norm + site * Ls + slo);
-    nhi *= __ldg(p.in_norm + site * Ls + shi);
+    nlo *= __ldg(cnorm + site * Ls + slo);
+    nhi *= __ldg(cnorm + site * Ls + shi);
   }
-  const T a5 = T(p.a5);
+  const T a5 = T(p.a5), kh = T(p.khop);
 #pragma unroll
   for (int j = 0; j < N; ++j) {
 #pragma unroll
     for (int k = 0; k < 12; ++k) {
-      acc[j][k].r = a5 * cen[j][k].r - T(0.5) * acc[j][k].r;
-      acc[j][k].i = a5 * cen[j][k].i - T(0.5) * acc[j][k].i;
+      acc[j][k].r = a5 * cen[j][k].r - kh * acc[j][k].r;
+      acc[j][k].i = a5 * cen[j][k].i - kh * acc[j][k].i;
     }
 #pragma unroll
     for (int k = 0; k < 6; ++k) {

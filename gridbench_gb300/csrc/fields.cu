@@ -422,6 +422,7 @@ int gbdw_lattice_destroy(gbdw_lattice* lat) {
   cudaStreamSynchronize(stream());
   if (lat->nbr4) cudaFree(lat->nbr4);
   if (lat->nbr5) cudaFree(lat->nbr5);
+  if (lat->cbsite) cudaFree(lat->cbsite);
   delete lat;
   return GBDW_OK;
 }

@@ -177,6 +177,47 @@ int gbdw_cg_solve(const gbdw_gauge* g_double, const gbdw_gauge* g_single,
                   const gbdw_gauge* g_sloppy, gbdw_field* x, const gbdw_field* b, double M5,
                   double mf, int mode, const gbdw_cg_params* prm, gbdw_cg_stats* stats);
 
+/* ------------------------------------------------------------------ even-odd (red-black)
+ * The 4D checkerboard of the reference's red-black grids (TableGenerate.cc:26-28,
+ * makeFourDimRedBlackGrid / makeFiveDimRedBlackGrid).  No counterpart kernels exist in the
+ * reference; everything here follows from the full operator by restriction:
+ *   M = [[D5, -1/2 Dhop_eo], [-1/2 Dhop_oe, D5]],   D5 = the 5th-dimension (site-local) part,
+ *   Mpc = D5 - 1/4 Dhop_pq D5^-1 Dhop_qp on half p.
+ * Half lattices hold the sites of one parity of a periodic lattice with even extents,
+ * numbered parent_site / 2; half fields and half gauge fields live on them. */
+/* even (parity 0) and odd half of a lattice made by gbdw_lattice_create; destroy each half
+ * with gbdw_lattice_destroy */
+int gbdw_lattice_checkerboard(const gbdw_lattice* full, gbdw_lattice** even, gbdw_lattice** odd);
+/* the links of the half's sites, in half-site order (a copy; precision of `full`) */
+int gbdw_gauge_checkerboard(gbdw_gauge** out, const gbdw_gauge* full, const gbdw_lattice* half);
+/* half <- the half's parity of full ; full <- half on the half's parity (other sites kept) */
+int gbdw_field_pick(gbdw_field* half, const gbdw_field* full);
+int gbdw_field_place(gbdw_field* full, const gbdw_field* half);
+/* out (half p, on g's lattice) = Dhop_pq in (half q); dag: DhopDag_pq */
+int gbdw_dhop_eo(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag);
+/* out (half p) = D5 cen - khop Dhop_pq in (D5^dag, DhopDag for dag); khop 1/2 gives M's
+ * rows of parity p */
+int gbdw_dwf_meo(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, const gbdw_field* cen,
+                 double M5, double mf, int dag, double khop);
+/* out = D5^-1 in (D5^-dag for dag) in closed form; any lattice, single rhs, Ls <= 64 */
+int gbdw_dwf_m5inv(gbdw_field* out, const gbdw_field* in, double M5, double mf, int dag);
+/* out = Mpc in (Mpc^dag for dag) on half p = gp's lattice; tq1, tq2 temporaries on half q;
+ * |out|^2 into norm2 when non-null */
+int gbdw_dwf_mpc(const gbdw_gauge* gp, const gbdw_gauge* gq, gbdw_field* out, gbdw_field* tq1,
+                 gbdw_field* tq2, const gbdw_field* in, double M5, double mf, int dag, double* norm2);
+/* out = Mpc^dag Mpc in; tp on half p, tq1/tq2 on half q; pap = |Mpc in|^2 */
+int gbdw_dwf_mpcdagmpc(const gbdw_gauge* gp, const gbdw_gauge* gq, gbdw_field* out, gbdw_field* tp,
+                       gbdw_field* tq1, gbdw_field* tq2, const gbdw_field* in, double M5, double mf,
+                       double* pap);
+/* Solves M x = b (x, b F64 on the full lattice; x holds the initial guess) by CG on the odd
+ * Schur normal system with the modes and reliable updates of gbdw_cg_solve.  g_*[0] / [1]
+ * are the even / odd gauge halves (g_single for PLAIN, g_sloppy for MIXED).  tol is the
+ * target of the Schur normal system's true residual; stats->true_residual reports the full
+ * system's |b - M x| / |b|. */
+int gbdw_cg_solve_eo(const gbdw_gauge* const g_double[2], const gbdw_gauge* const g_single[2],
+                     const gbdw_gauge* const g_sloppy[2], gbdw_field* x, const gbdw_field* b,
+                     double M5, double mf, int mode, const gbdw_cg_params* prm, gbdw_cg_stats* stats);
+
 /* ------------------------------------------------------------------ batched persistent Dhop
  * Many independent instances (own lattice, gauge field, Ls and precision) in one persistent
  * launch, replayed through a CUDA graph. */
