@@ -16,7 +16,9 @@
 // (S psi)(0) = -mf psi(Ls-1); on spins 2,3 the shift runs the other way (s+1, wrap at Ls-1);
 // dag swaps the two.  S^Ls = -mf, so (a5 - S) sum_{j<Ls} S^j a5^-(j+1) = (1 + mf a5^-Ls),
 // i.e.  D5^-1 = g sum_{j<Ls} a5^-j S^j  with  g = 1 / (a5 (1 + mf a5^-Ls)):  a dense Ls x Ls
-// matrix per chirality whose entries are g a5^-j (no wrap) or -mf g a5^-j (one wrap).
+// matrix per chirality whose entries are g a5^-j (no wrap) or -mf g a5^-j (one wrap), applied
+// in O(Ls) per row as a first-order recursion (k_m5inv).
+#include <algorithm>
 #include <cmath>
 
 #include "blas.h"
@@ -83,57 +85,85 @@ struct M5InvParams {
   int64_t nsite;
   int Ls;
   int LsP;
+  int nsb;        // sites per CTA
+  double ia5;     // 1 / a5
+  double g;       // 1 / (a5 (1 + mf a5^-Ls))
   double mf;
-  double c[kMaxLsInv];  // g a5^-j
 };
 
-// One thread per (site, N consecutive slices); all Ls input slices of the site are read.
+// The recursion form of D5^-1 on one chirality, per spin-colour row (x, y of length Ls):
+//   shift s-1 -> s:  y(0) = g [x(0) - mf sum_{t>=1} a5^-(Ls-t) x(t)],  y(s) = (x(s) + y(s-1)) / a5
+//   shift s+1 -> s:  y(Ls-1) = g [x(Ls-1) - mf sum_{t<=Ls-2} a5^-(t+1) x(t)],  y(s) = (x(s) + y(s+1)) / a5
+// which is the dense form above row by row (the wrap coefficient folds into g).  Phase 1:
+// one thread per (site, row) runs both sweeps into a shared-memory tile; phase 2: one thread
+// per (site, N slices) writes the tile in the field's storage format (norms for F16).
 template <int P, int DAG, int N>
-__global__ void __launch_bounds__(256) k_m5inv(const M5InvParams p) {
+__global__ void __launch_bounds__(192) k_m5inv(const M5InvParams p) {
   using T = typename Arith<P>::T;
-  __shared__ T cs[kMaxLsInv];
-  for (int j = threadIdx.x; j < p.Ls; j += blockDim.x) cs[j] = T(p.c[j]);
-  __syncthreads();
-  const int G = p.Ls / N;
-  const int64_t tid = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (tid >= p.nsite * G) return;
-  const int64_t site = tid / G;
-  const int s0 = int(tid - site * G) * N;
-  const int64_t row0 = site * 12;
-  cpx<T> acc[N][12];
-#pragma unroll
-  for (int j = 0; j < N; ++j)
-#pragma unroll
-    for (int k = 0; k < 12; ++k) acc[j][k] = {T(0), T(0)};
-  const T mf = T(-p.mf);
-  for (int t = 0; t < p.Ls; ++t) {
-    cpx<T> x[12];
-#pragma unroll
-    for (int k = 0; k < 12; ++k) x[k] = Elem<P>::ld(p.in, row0 + k, t, p.LsP);
-    if constexpr (P == GBDW_F16) {
-      const float n = __ldg(p.in_norm + site * p.Ls + t);
-#pragma unroll
-      for (int k = 0; k < 12; ++k) x[k] = {x[k].r * n, x[k].i * n};
-    }
-#pragma unroll
-    for (int j = 0; j < N; ++j) {
-      const int s = s0 + j;
-      // shift towards larger s (psi(s-1) feeds s): source t reaches s after s - t steps
-      const T cdn = t <= s ? cs[s - t] : mf * cs[s - t + p.Ls];
-      // shift towards smaller s: t reaches s after t - s steps
-      const T cup = t >= s ? cs[t - s] : mf * cs[t - s + p.Ls];
-      const T cu = DAG ? cup : cdn;  // spins 0,1
-      const T cl = DAG ? cdn : cup;  // spins 2,3
-#pragma unroll
-      for (int k = 0; k < 6; ++k) {
-        acc[j][k].r += cu * x[k].r;
-        acc[j][k].i += cu * x[k].i;
-        acc[j][6 + k].r += cl * x[6 + k].r;
-        acc[j][6 + k].i += cl * x[6 + k].i;
+  extern __shared__ __align__(16) unsigned char m5_smem[];
+  cpx<T>* tile = reinterpret_cast<cpx<T>*>(m5_smem);  // [nsb][12][Ls + 1] (padded rows)
+  const int Ls = p.Ls, LsT = p.Ls + 1;
+  const int64_t site0 = int64_t(blockIdx.x) * p.nsb;
+  const T ia5 = T(p.ia5), g = T(p.g), mf = T(p.mf);
+  if (threadIdx.x < 12 * p.nsb) {
+    const int ls = threadIdx.x / 12, row = threadIdx.x - 12 * (threadIdx.x / 12);
+    const int64_t site = site0 + ls;
+    if (site < p.nsite) {
+      const int64_t r = site * 12 + row;
+      auto x = [&](int t) -> cpx<T> {
+        cpx<T> v = Elem<P>::ld(p.in, r, t, p.LsP);
+        if constexpr (P == GBDW_F16) {
+          const float n = __ldg(p.in_norm + site * Ls + t);
+          v = {v.r * n, v.i * n};
+        }
+        return v;
+      };
+      cpx<T>* y = tile + (ls * 12 + row) * LsT;
+      const bool down = (row < 6) != (DAG != 0);  // psi(s-1) feeds s
+      cpx<T> w = {T(0), T(0)};
+      if (down) {
+        for (int t = 1; t < Ls; ++t) {
+          const cpx<T> v = x(t);
+          w = {(w.r + v.r) * ia5, (w.i + v.i) * ia5};
+        }
+        const cpx<T> x0 = x(0);
+        cpx<T> prev = {g * (x0.r - mf * w.r), g * (x0.i - mf * w.i)};
+        y[0] = prev;
+        for (int t = 1; t < Ls; ++t) {
+          const cpx<T> v = x(t);
+          prev = {(v.r + prev.r) * ia5, (v.i + prev.i) * ia5};
+          y[t] = prev;
+        }
+      } else {
+        for (int t = Ls - 2; t >= 0; --t) {
+          const cpx<T> v = x(t);
+          w = {(w.r + v.r) * ia5, (w.i + v.i) * ia5};
+        }
+        const cpx<T> xl = x(Ls - 1);
+        cpx<T> prev = {g * (xl.r - mf * w.r), g * (xl.i - mf * w.i)};
+        y[Ls - 1] = prev;
+        for (int t = Ls - 2; t >= 0; --t) {
+          const cpx<T> v = x(t);
+          prev = {(v.r + prev.r) * ia5, (v.i + prev.i) * ia5};
+          y[t] = prev;
+        }
       }
     }
   }
-  store_spinor<P, N>(p.out, p.out_norm, site, s0, p.Ls, p.LsP, acc);
+  __syncthreads();
+  const int G = Ls / N;
+  for (int it = threadIdx.x; it < p.nsb * G; it += blockDim.x) {
+    const int ls = it / G;
+    const int64_t site = site0 + ls;
+    if (site >= p.nsite) break;
+    const int s0 = (it - ls * G) * N;
+    cpx<T> v[N][12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k)
+#pragma unroll
+      for (int j = 0; j < N; ++j) v[j][k] = tile[(ls * 12 + k) * LsT + s0 + j];
+    store_spinor<P, N>(p.out, p.out_norm, site, s0, Ls, p.LsP, v);
+  }
 }
 
 bool is_half(const gbdw_lattice* l) { return l && l->parity >= 0 && l->cbsite; }
@@ -160,27 +190,27 @@ int m5inv(gbdw_field* out, const gbdw_field* in, double M5, double mf, int dag) 
   p.Ls = Ls;
   p.LsP = in->LsP;
   p.mf = mf;
+  p.ia5 = 1.0 / a5;
   const double den = a5 * (1.0 + mf * std::pow(a5, -double(Ls)));
   if (!(std::fabs(den) > 0.0) || !std::isfinite(den)) {
     set_error("D5^-1: singular 5th-dimension operator for these M5, mf");
     return GBDW_ERR_INVALID;
   }
-  double c = 1.0 / den;
-  for (int j = 0; j < kMaxLsInv; ++j) {
-    p.c[j] = j < Ls ? c : 0.0;
-    c /= a5;
-  }
+  p.g = 1.0 / den;
   if (int st = ensure_device()) return st;
+  const size_t per_site = 12 * size_t(Ls + 1) * (in->prec == GBDW_F64 ? 16 : 8);
+  p.nsb = int(std::min<size_t>(16, 49152 / per_site));
+  const size_t smem = size_t(p.nsb) * per_site;
+  const unsigned g = nb(p.nsite, p.nsb);
+  const int threads = 12 * p.nsb;
   const bool pair = Ls % 2 == 0;
-  const int64_t n = p.nsite * (pair ? Ls / 2 : Ls);
-  const unsigned g = nb(n, 128);
 #define GBDW_M5(P)                                                                               \
   if (pair) {                                                                                    \
-    if (dag) k_m5inv<P, 1, 2><<<g, 128, 0, stream()>>>(p);                                       \
-    else k_m5inv<P, 0, 2><<<g, 128, 0, stream()>>>(p);                                           \
+    if (dag) k_m5inv<P, 1, 2><<<g, threads, smem, stream()>>>(p);                                \
+    else k_m5inv<P, 0, 2><<<g, threads, smem, stream()>>>(p);                                    \
   } else {                                                                                       \
-    if (dag) k_m5inv<P, 1, 1><<<g, 128, 0, stream()>>>(p);                                       \
-    else k_m5inv<P, 0, 1><<<g, 128, 0, stream()>>>(p);                                           \
+    if (dag) k_m5inv<P, 1, 1><<<g, threads, smem, stream()>>>(p);                                \
+    else k_m5inv<P, 0, 1><<<g, threads, smem, stream()>>>(p);                                    \
   }
   if (in->prec == GBDW_F64) {
     GBDW_M5(GBDW_F64)
