@@ -97,12 +97,37 @@ struct M5InvParams {
 // which is the dense form above row by row (the wrap coefficient folds into g).  Phase 1:
 // one thread per (site, row) runs both sweeps into a shared-memory tile; phase 2: one thread
 // per (site, N slices) writes the tile in the field's storage format (norms for F16).
-template <int P, int DAG, int N>
+// Both sweeps of one row over values v[0..Ls) (registers when LSC > 0), results into y.
+template <class T, bool DOWN, class V>
+__device__ __forceinline__ void m5_sweeps(const V& v, int Ls, T ia5, T g, T mf, cpx<T>* y) {
+  cpx<T> w = {T(0), T(0)};
+  if constexpr (DOWN) {
+    for (int t = 1; t < Ls; ++t) w = {(w.r + v(t).r) * ia5, (w.i + v(t).i) * ia5};
+    cpx<T> prev = {g * (v(0).r - mf * w.r), g * (v(0).i - mf * w.i)};
+    y[0] = prev;
+    for (int t = 1; t < Ls; ++t) {
+      prev = {(v(t).r + prev.r) * ia5, (v(t).i + prev.i) * ia5};
+      y[t] = prev;
+    }
+  } else {
+    for (int t = Ls - 2; t >= 0; --t) w = {(w.r + v(t).r) * ia5, (w.i + v(t).i) * ia5};
+    cpx<T> prev = {g * (v(Ls - 1).r - mf * w.r), g * (v(Ls - 1).i - mf * w.i)};
+    y[Ls - 1] = prev;
+    for (int t = Ls - 2; t >= 0; --t) {
+      prev = {(v(t).r + prev.r) * ia5, (v(t).i + prev.i) * ia5};
+      y[t] = prev;
+    }
+  }
+}
+
+// LSC > 0: the launch guarantees Ls == LSC (even), and a row is loaded into registers with
+// slice-pair vector loads before the sweeps; LSC == 0 reads the row slice by slice.
+template <int P, int DAG, int N, int LSC>
 __global__ void __launch_bounds__(192) k_m5inv(const M5InvParams p) {
   using T = typename Arith<P>::T;
   extern __shared__ __align__(16) unsigned char m5_smem[];
   cpx<T>* tile = reinterpret_cast<cpx<T>*>(m5_smem);  // [nsb][12][Ls + 1] (padded rows)
-  const int Ls = p.Ls, LsT = p.Ls + 1;
+  const int Ls = LSC > 0 ? LSC : p.Ls, LsT = Ls + 1;
   const int64_t site0 = int64_t(blockIdx.x) * p.nsb;
   const T ia5 = T(p.ia5), g = T(p.g), mf = T(p.mf);
   if (threadIdx.x < 12 * p.nsb) {
@@ -110,43 +135,37 @@ __global__ void __launch_bounds__(192) k_m5inv(const M5InvParams p) {
     const int64_t site = site0 + ls;
     if (site < p.nsite) {
       const int64_t r = site * 12 + row;
-      auto x = [&](int t) -> cpx<T> {
-        cpx<T> v = Elem<P>::ld(p.in, r, t, p.LsP);
-        if constexpr (P == GBDW_F16) {
-          const float n = __ldg(p.in_norm + site * Ls + t);
-          v = {v.r * n, v.i * n};
-        }
-        return v;
-      };
       cpx<T>* y = tile + (ls * 12 + row) * LsT;
       const bool down = (row < 6) != (DAG != 0);  // psi(s-1) feeds s
-      cpx<T> w = {T(0), T(0)};
-      if (down) {
-        for (int t = 1; t < Ls; ++t) {
-          const cpx<T> v = x(t);
-          w = {(w.r + v.r) * ia5, (w.i + v.i) * ia5};
+      if constexpr (LSC > 0) {
+        cpx<T> xv[LSC];
+#pragma unroll
+        for (int q = 0; q < LSC / 2; ++q) {
+          cpx<T> v2[2];
+          Vec<P, 2>::load(p.in, r, 2 * q, p.LsP, v2);
+          xv[2 * q] = v2[0];
+          xv[2 * q + 1] = v2[1];
         }
-        const cpx<T> x0 = x(0);
-        cpx<T> prev = {g * (x0.r - mf * w.r), g * (x0.i - mf * w.i)};
-        y[0] = prev;
-        for (int t = 1; t < Ls; ++t) {
-          const cpx<T> v = x(t);
-          prev = {(v.r + prev.r) * ia5, (v.i + prev.i) * ia5};
-          y[t] = prev;
+        if constexpr (P == GBDW_F16) {
+          float nr[LSC];
+          load_norms<LSC>(p.in_norm, site * LSC, nr);
+#pragma unroll
+          for (int t = 0; t < LSC; ++t) xv[t] = {xv[t].r * nr[t], xv[t].i * nr[t]};
         }
+        auto v = [&](int t) -> const cpx<T>& { return xv[t]; };
+        if (down) m5_sweeps<T, true>(v, LSC, ia5, g, mf, y);
+        else m5_sweeps<T, false>(v, LSC, ia5, g, mf, y);
       } else {
-        for (int t = Ls - 2; t >= 0; --t) {
-          const cpx<T> v = x(t);
-          w = {(w.r + v.r) * ia5, (w.i + v.i) * ia5};
-        }
-        const cpx<T> xl = x(Ls - 1);
-        cpx<T> prev = {g * (xl.r - mf * w.r), g * (xl.i - mf * w.i)};
-        y[Ls - 1] = prev;
-        for (int t = Ls - 2; t >= 0; --t) {
-          const cpx<T> v = x(t);
-          prev = {(v.r + prev.r) * ia5, (v.i + prev.i) * ia5};
-          y[t] = prev;
-        }
+        auto v = [&](int t) -> cpx<T> {
+          cpx<T> e = Elem<P>::ld(p.in, r, t, p.LsP);
+          if constexpr (P == GBDW_F16) {
+            const float n = __ldg(p.in_norm + site * Ls + t);
+            e = {e.r * n, e.i * n};
+          }
+          return e;
+        };
+        if (down) m5_sweeps<T, true>(v, Ls, ia5, g, mf, y);
+        else m5_sweeps<T, false>(v, Ls, ia5, g, mf, y);
       }
     }
   }
@@ -205,12 +224,15 @@ int m5inv(gbdw_field* out, const gbdw_field* in, double M5, double mf, int dag) 
   const int threads = 12 * p.nsb;
   const bool pair = Ls % 2 == 0;
 #define GBDW_M5(P)                                                                               \
-  if (pair) {                                                                                    \
-    if (dag) k_m5inv<P, 1, 2><<<g, threads, smem, stream()>>>(p);                                \
-    else k_m5inv<P, 0, 2><<<g, threads, smem, stream()>>>(p);                                    \
+  if (Ls == 16) {                                                                                \
+    if (dag) k_m5inv<P, 1, 2, 16><<<g, threads, smem, stream()>>>(p);                            \
+    else k_m5inv<P, 0, 2, 16><<<g, threads, smem, stream()>>>(p);                                \
+  } else if (pair) {                                                                             \
+    if (dag) k_m5inv<P, 1, 2, 0><<<g, threads, smem, stream()>>>(p);                             \
+    else k_m5inv<P, 0, 2, 0><<<g, threads, smem, stream()>>>(p);                                 \
   } else {                                                                                       \
-    if (dag) k_m5inv<P, 1, 1><<<g, threads, smem, stream()>>>(p);                                \
-    else k_m5inv<P, 0, 1><<<g, threads, smem, stream()>>>(p);                                    \
+    if (dag) k_m5inv<P, 1, 1, 0><<<g, threads, smem, stream()>>>(p);                             \
+    else k_m5inv<P, 0, 1, 0><<<g, threads, smem, stream()>>>(p);                                 \
   }
   if (in->prec == GBDW_F64) {
     GBDW_M5(GBDW_F64)

@@ -78,8 +78,10 @@ def test_dhop_eo_is_restricted_full_dhop(gpu, prec, dag):
 
 @pytest.mark.parametrize("prec", [gb.F64, gb.F32, gb.F16])
 @pytest.mark.parametrize("dag", [0, 1])
-def test_m5inv_inverts_the_fifth_dimension_operator(gpu, prec, dag):
-    dims, Ls = (2, 2, 2, 4), 8
+@pytest.mark.parametrize("Ls", [8, 16])
+def test_m5inv_inverts_the_fifth_dimension_operator(gpu, prec, dag, Ls):
+    """Ls = 16 takes the register-resident form of the kernel, other extents the general one."""
+    dims = (2, 2, 2, 4)
     c = make_case(dims, Ls)
     lat = gb.Lattice.periodic(dims, Ls)
     x = gb.Field(lat, prec).load(c["phi"])
@@ -89,7 +91,7 @@ def test_m5inv_inverts_the_fifth_dimension_operator(gpu, prec, dag):
     assert rel_err(back, x.numpy()) < TOL[prec]
 
 
-@pytest.mark.parametrize("Ls", [5, 12])
+@pytest.mark.parametrize("Ls", [1, 5, 12, 64])
 def test_m5inv_odd_and_even_ls(gpu, Ls):
     dims = (2, 2, 2, 2)
     c = make_case(dims, Ls)
