@@ -242,6 +242,33 @@ def dwf_mdagm(g: Gauge, out: Field, tmp: Field, inp: Field, M5: float, mf: float
     return v.value
 
 
+def read_static_data(h_path: str, cc_path: str) -> dict:
+    """A static_data.h / static_data.cc pair in the reference's format: nsite (outer sites), Ls,
+    nsimd and the arrays U, Phi, Psi (the reference result), nbr, prm."""
+    L = load()
+    ns, ls, nsimd = C.c_uint64(), C.c_int(), C.c_int()
+    cnt = (C.c_uint64 * 5)()
+    check(L.gbdw_static_data_info(h_path.encode(), cc_path.encode(), C.byref(ns), C.byref(ls), C.byref(nsimd), cnt))
+    U, Phi, Psi = (np.empty(cnt[k], np.float64) for k in range(3))
+    nbr, prm = np.empty(cnt[3], np.uint64), np.empty(cnt[4], np.uint8)
+    check(L.gbdw_static_data_read(cc_path.encode(), _ptr(U), cnt[0], _ptr(Phi), cnt[1], _ptr(Psi), cnt[2],
+                                  _ptr(nbr), cnt[3], _ptr(prm), cnt[4]))
+    return {"nsite": ns.value, "Ls": ls.value, "nsimd": nsimd.value, "U": U, "Phi": Phi, "Psi": Psi,
+            "nbr": nbr, "prm": prm}
+
+
+def write_static_data(h_path: str, cc_path: str, nsite: int, Ls: int, U, Phi, Psi, nbr, prm, nsimd: int = 1):
+    """Writes arrays as a static_data.h / static_data.cc pair the reference's benchmarks compile."""
+    U, Phi, Psi = (np.ascontiguousarray(a, dtype=np.float64) for a in (U, Phi, Psi))
+    nbr = np.ascontiguousarray(nbr, dtype=np.uint64)
+    prm = np.ascontiguousarray(prm, dtype=np.uint8)
+    if (U.size != nsite * 144 * nsimd or Phi.size != nsite * Ls * 24 * nsimd or Psi.size != Phi.size
+            or nbr.size != nsite * Ls * 8 or prm.size != nbr.size):
+        raise ValueError("array lengths disagree with nsite, Ls and nsimd")
+    check(load().gbdw_static_data_write(h_path.encode(), cc_path.encode(), nsite, Ls, nsimd, _ptr(U), _ptr(Phi),
+                                        _ptr(Psi), _ptr(nbr), _ptr(prm)))
+
+
 def dhop_eo(g: Gauge, out: Field, inp: Field, dag: int = 0) -> None:
     """out (g's half lattice) = Dhop from the partner half's inp"""
     check(load().gbdw_dhop_eo(g.h, out.h, inp.h, int(dag)))

@@ -88,6 +88,10 @@ PROTOTYPES = {
     "gbdw_dwf_mpc": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _d, _d, _i, _dp]),
     "gbdw_dwf_mpcdagmpc": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, _d, _dp]),
     "gbdw_cg_solve_eo": (_i, [_pp, _pp, _pp, _vp, _vp, _d, _d, _i, C.POINTER(CGParams), C.POINTER(CGStats)]),
+    "gbdw_static_data_info": (_i, [C.c_char_p, C.c_char_p, C.POINTER(C.c_uint64), C.POINTER(C.c_int),
+                                   C.POINTER(C.c_int), C.POINTER(C.c_uint64)]),
+    "gbdw_static_data_read": (_i, [C.c_char_p, _vp, _u64, _vp, _u64, _vp, _u64, _vp, _u64, _vp, _u64]),
+    "gbdw_static_data_write": (_i, [C.c_char_p, C.c_char_p, _u64, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     "gbdw_batch_create": (_i, [_pp, _i, _pp, _pp, _pp, _i]),
     "gbdw_batch_run": (_i, [_vp]),
     "gbdw_batch_destroy": (_i, [_vp]),

@@ -218,6 +218,25 @@ int gbdw_cg_solve_eo(const gbdw_gauge* const g_double[2], const gbdw_gauge* cons
                      const gbdw_gauge* const g_sloppy[2], gbdw_field* x, const gbdw_field* b,
                      double M5, double mf, int mode, const gbdw_cg_params* prm, gbdw_cg_stats* stats);
 
+/* ------------------------------------------------------------------ static-data files
+ * The reference's exchange format for Grid-generated test data (TableGenerate.cc:93-138,
+ * read by bench.cc:55-88 and bench_simple.cc:72-84 as compiled-in arrays): static_data.h holds
+ * `nsite` (outer sites) and `Ls`, static_data.cc the arrays U_static (nsite*144*Nsimd doubles,
+ * the doubled gauge field), Phi_static and Psi_cpp_static (nsite*Ls*24*Nsimd doubles, source
+ * and reference Dhop result), nbr_static (uint64) and prm_static (uint8), nsite*Ls*8 each,
+ * every array closed by a sentinel 0.  Host-only; no device needed. */
+/* sizes of a file pair: counts = entries of U, Phi, Psi_cpp, nbr, prm (sentinels excluded) */
+int gbdw_static_data_info(const char* h_path, const char* cc_path, uint64_t* nsite, int* Ls,
+                          int* nsimd, uint64_t counts[5]);
+/* reads the five arrays into caller buffers whose lengths must equal the counts above */
+int gbdw_static_data_read(const char* cc_path, double* U, uint64_t nU, double* Phi, uint64_t nPhi,
+                          double* Psi, uint64_t nPsi, uint64_t* nbr, uint64_t nnbr, uint8_t* prm,
+                          uint64_t nprm);
+/* writes a file pair in the reference's layout (doubles as %16.8le: 9 significant digits) */
+int gbdw_static_data_write(const char* h_path, const char* cc_path, uint64_t nsite, int Ls, int nsimd,
+                           const double* U, const double* Phi, const double* Psi,
+                           const uint64_t* nbr, const uint8_t* prm);
+
 /* ------------------------------------------------------------------ batched persistent Dhop
  * Many independent instances (own lattice, gauge field, Ls and precision) in one persistent
  * launch, replayed through a CUDA graph. */

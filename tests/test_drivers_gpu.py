@@ -46,3 +46,21 @@ def test_bench_simple_flow_driver(exes, tmp_path):
                         "--ref", str(p)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "normdiff" in r.stdout
+
+
+def test_dropin_kernel_on_a_static_data_file(gpu, tmp_path):
+    """The flow of bench_simple.cc on data read from a static_data.h / .cc pair: the drop-in
+    seam reproduces the file's reference result to the 9 digits the format keeps."""
+    import gridbench_gb300 as gb
+    from conftest import rel_err
+    dims, Ls = (4, 4, 2, 2), 8
+    U = gb.generate_gauge(dims)
+    phi = gb.generate_fermion(dims, Ls)
+    nbr, prm, nsite = gb.generate_table(dims, Ls)
+    psi = oracle.dslash(U, phi, nbr, prm, nsite, Ls)
+    h, cc = str(tmp_path / "static_data.h"), str(tmp_path / "static_data.cc")
+    gb.write_static_data(h, cc, nsite, Ls, U, phi, psi, nbr, prm)
+    d = gb.read_static_data(h, cc)
+    out = np.zeros_like(d["Phi"])
+    gb.dslash_kernel(1, d["U"], out, d["Phi"], d["nbr"], d["nsite"], d["Ls"], d["prm"])
+    assert rel_err(out, d["Psi"]) < 1e-7
