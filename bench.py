@@ -468,7 +468,8 @@ def run_ours(args, D: Dist) -> dict | None:
                    "l2": "inputs larger than L2: two alternating in/out pairs, 476 MB vs 129 MB L2",
                    "launch": {"threads": cfg[0], "slices_per_thread": cfg[1],
                               "form": {0: "direct", 1: "tma-staged (CTA ring)", 2: "tma-staged (warp rings)",
-                                       3: "direct (Ls=16 specialised)"}[cfg[2]],
+                                       3: "direct (Ls=16 specialised)",
+                                       4: "direct (Ls=16, 2^4 site blocks)"}[cfg[2]],
                               "stages": cfg[3]}},
         "rel_err_vs_fp64": rel,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",

@@ -356,7 +356,7 @@ def tune_dhop(g: Gauge, out: Field, inp: Field, dag: int = 0) -> tuple:
 
 def tune_query(g: Gauge, inp: Field) -> tuple:
     """(threads per CTA, slices per thread, form, stages); form 0 direct loads, 1 TMA-staged
-    CTA ring, 2 TMA-staged ring per warp, 3 direct FP32/FP16 kernel specialised for Ls*nrhs = 16."""
+    CTA ring, 2 TMA-staged ring per warp, 3 direct FP32/FP16 kernel specialised for Ls*nrhs = 16, 4 the same over 2x2x2x2 site blocks."""
     cfg = (C.c_int * 4)()
     check(load().gbdw_tune_query(g.h, inp.h, cfg))
     return tuple(int(v) for v in cfg)

@@ -40,6 +40,13 @@ int check_operands(const gbdw_gauge* g, const gbdw_field* out, const gbdw_field*
   return GBDW_OK;
 }
 
+bool blocked_ok(const gbdw_lattice* lat, const gbdw_field* in) {
+  if (in->prec == GBDW_F64 || in->LsE != 16 || in->LsP != 16 || lat->parity >= 0 || !lat->fast) return false;
+  for (int d = 0; d < 4; ++d)
+    if (lat->dims[d] <= 0 || lat->dims[d] % 2) return false;
+  return true;
+}
+
 DhopParams make_params(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in) {
   DhopParams p;
   p.U = g->d;
@@ -59,6 +66,7 @@ DhopParams make_params(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* i
   p.counter = nullptr;
   p.result = nullptr;
   p.err = device_error_word();
+  for (int d = 0; d < 4; ++d) p.dims[d] = g->lat->parity < 0 ? g->lat->dims[d] : 0;
   return p;
 }
 
@@ -92,6 +100,8 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
   if (staged && !tma_shape(in->prec, in->LsE, L, &NS, &tthreads, &smem)) L.mode = 0;
   if (L.mode == 3 && (in->prec == GBDW_F64 || L.spt != 2 || in->LsE != 16 || in->LsP != 16)) L.mode = 0;
   if (L.mode == 3) L.threads = 64;
+  if (L.mode == 4 && !blocked_ok(g->lat, in)) L.mode = 3;
+  if (L.mode == 4) L.threads = 128;
   const int64_t nthreads = p.nsite * (p.LsE / L.spt);
   const int64_t blocks = staged ? (p.nsite + NS - 1) / NS : (nthreads + L.threads - 1) / L.threads;
   Reduce red;
@@ -117,7 +127,7 @@ bool tma_shape(int prec, int LsE, DhopLaunch L, int* NS, int* threads, size_t* s
   const size_t esz = spinor_elem_bytes(prec);
   const size_t blk = 12 * size_t(padded_slices(prec, LsE)) * esz + (prec == GBDW_F16 ? 4 * size_t(LsE) : 0);
   const size_t lb = 8 * link_bytes(prec);
-  if (L.mode == 3) return false;  // a direct form: no staging shape
+  if (L.mode == 3 || L.mode == 4) return false;  // direct forms: no staging shape
   if (L.mode == 2) {
     // one ring per warp: a warp owns 32/Tps whole sites
     if (Tps > 32 || L.threads % 32 != 0 || L.threads > 256) return false;

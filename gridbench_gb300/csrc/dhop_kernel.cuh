@@ -386,6 +386,7 @@ struct DhopParams {
   const void* cen = nullptr;
   const float* cen_norm = nullptr;
   double khop = 0.5;
+  int dims[4] = {0, 0, 0, 0};  // periodic lattice extents (the blocked site order needs them)
 };
 
 // Writes N slices of v[N][12] (slices e0.., norms for F16); returns the sum of squares of
@@ -542,8 +543,11 @@ __device__ __forceinline__ void dhop_thread(const DhopParams& p, unsigned site, 
 // MINB > 0 caps registers so that MINB CTAs of up to MAXT threads fit on an SM (more warps,
 // more loads in flight); MINB = 0 leaves the compiler free up to 256 threads.
 // LSPC > 0: the launch guarantees LsE == LsP == LSPC, so every row offset is a compile-time
-// constant.
-template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int MINB = 0, int LSPC = 0, int MAXT = 128>
+// constant.  BLK: a CTA of 16*G threads takes a 2x2x2x2 block of 4D sites instead of 16
+// consecutive ones, so half of every site's neighbours are the CTA's own sites and their
+// loads can hit L1 (needs a periodic lattice with even extents, p.dims).
+template <int PIN, int POUT, int GP, int DAG, int N, int EPI, int MINB = 0, int LSPC = 0, int MAXT = 128,
+          int BLK = 0>
 __global__ void __launch_bounds__(MINB > 0 ? MAXT : 256, MINB > 0 ? MINB : 1) k_dhop(const DhopParams p_) {
   using T = typename Arith<PIN>::T;
   DhopParams p = p_;
@@ -557,8 +561,22 @@ __global__ void __launch_bounds__(MINB > 0 ? MAXT : 256, MINB > 0 ? MINB : 1) k_
   float part = 0.f;
   double dpart = 0.0;
   if (active) {
-    const unsigned site = tid / G;
+    unsigned site = tid / G;
     const int s0 = int(tid - site * G) * N;
+    if constexpr (BLK) {
+      const unsigned l = threadIdx.x / G;  // 0..15 inside the block
+      const unsigned hx = unsigned(p.dims[0]) >> 1, hy = unsigned(p.dims[1]) >> 1, hz = unsigned(p.dims[2]) >> 1;
+      unsigned b = blockIdx.x;
+      const unsigned bx = b % hx;
+      b /= hx;
+      const unsigned by = b % hy;
+      b /= hy;
+      const unsigned bz = b % hz;
+      const unsigned bt = b / hz;
+      const unsigned x = 2 * bx + (l & 1), y = 2 * by + ((l >> 1) & 1), z = 2 * bz + ((l >> 2) & 1),
+                     t = 2 * bt + (l >> 3);
+      site = x + unsigned(p.dims[0]) * (y + unsigned(p.dims[1]) * (z + unsigned(p.dims[2]) * t));
+    }
     cpx<T> acc[N][12];
     dhop_thread<PIN, GP, DAG, N>(p, site, s0, acc);
     if constexpr (EPI == 1) dwf_epilogue<PIN, DAG, N>(p, site, s0, acc);
@@ -605,6 +623,7 @@ struct DhopLaunch {
   int spt;         // slices per thread
   int mode = 0;    // 0: direct loads, 1: TMA-staged (CTA ring), 2: TMA-staged (one ring per warp),
                    // 3: direct, FP32/FP16 Ls = 16 at compile time, registers balanced for 6 CTAs/SM
+                   // 4: form 3 on 2x2x2x2 site blocks per 128-thread CTA (periodic, even extents)
   int stages = 4;  // staged kernels: depth of the leg ring
 };
 

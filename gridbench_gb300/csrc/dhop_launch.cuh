@@ -87,6 +87,14 @@ int by_shape(const DhopParams& p, DhopLaunch L) {
         return GBDW_OK;
       }
     }
+  } else if (L.mode == 4) {
+    if constexpr (PIN == GBDW_F32 || PIN == GBDW_F16) {
+      if (L.spt == 2 && p.LsE == 16 && p.LsP == 16 && p.nsite % 16 == 0) {
+        k_dhop<PIN, POUT, GP, DAG, 2, EPI, 3, 16, 128, 1><<<unsigned(p.nsite / 16), 128, 0, stream()>>>(p);
+        GBDW_LAUNCHED();
+        return GBDW_OK;
+      }
+    }
   } else if (L.mode == 2) {
     if (L.spt == S1) return L.stages == 2 ? go_tmaw<PIN, POUT, GP, DAG, S1, EPI, 2>(p, L) : go_tmaw<PIN, POUT, GP, DAG, S1, EPI, 4>(p, L);
     if (L.spt == S2) return L.stages == 2 ? go_tmaw<PIN, POUT, GP, DAG, S2, EPI, 2>(p, L) : go_tmaw<PIN, POUT, GP, DAG, S2, EPI, 4>(p, L);

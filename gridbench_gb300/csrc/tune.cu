@@ -77,6 +77,7 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
         }
   }
   if (in->prec != GBDW_F64 && in->LsE == 16 && in->LsP == 16) cands.push_back(DhopLaunch{64, 2, 3, 4});
+  if (blocked_ok(g->lat, in)) cands.push_back(DhopLaunch{128, 2, 4, 4});
   cudaEvent_t a, b;
   GBDW_CUDA(cudaEventCreate(&a));
   GBDW_CUDA(cudaEventCreate(&b));
@@ -121,15 +122,20 @@ int gbdw_tune_query(const gbdw_gauge* g, const gbdw_field* in, int cfg[4]) {
 
 int gbdw_tune_set(const gbdw_gauge* g, const gbdw_field* in, int threads, int spt, int form, int stages) {
   if (!g || !in || threads < 32 || threads > 256 || threads % 32 != 0 || !(spt == 1 || spt == 2 || spt == 4) ||
-      in->LsE % spt != 0 || (in->prec == GBDW_F64 && spt > 2) || form < 0 || form > 3 ||
+      in->LsE % spt != 0 || (in->prec == GBDW_F64 && spt > 2) || form < 0 || form > 4 ||
       (stages != 2 && stages != 4)) {
     set_error("gbdw_tune_set: threads 32..256 in steps of 32, spt 1/2/4 dividing Ls*nrhs (<= 2 for F64), "
-              "form 0..3, stages 2/4");
+              "form 0..4, stages 2/4");
     return GBDW_ERR_INVALID;
   }
   const DhopLaunch L{threads, spt, form, stages};
   if (form == 3 && (spt != 2 || in->prec == GBDW_F64 || in->LsE != 16 || in->LsP != 16)) {
     set_error("gbdw_tune_set: form 3 is the FP32/FP16 Ls*nrhs = 16 kernel with 2 slices per thread");
+    return GBDW_ERR_INVALID;
+  }
+  if (form == 4 && (spt != 2 || !blocked_ok(g->lat, in))) {
+    set_error("gbdw_tune_set: form 4 needs FP32/FP16, Ls*nrhs = 16, 2 slices per thread and a periodic lattice "
+              "with even extents");
     return GBDW_ERR_INVALID;
   }
   if (form == 1 || form == 2) {
@@ -190,7 +196,7 @@ int gbdw_tune_load(const char* path) {
     if (lb == std::string::npos) break;
     if (sscanf(key.c_str(), "g%d_s%d_L%d_e%d", &gp, &sp, &LsE, &epi) == 4 &&
         sscanf(text.c_str() + lb, "[%d , %d , %d , %d]", &th, &spt, &mode, &stages) >= 2 && th > 0 && th <= 256 &&
-        th % 32 == 0 && (spt == 1 || spt == 2 || spt == 4) && mode >= 0 && mode <= 3 && (stages == 2 || stages == 4)) {
+        th % 32 == 0 && (spt == 1 || spt == 2 || spt == 4) && mode >= 0 && mode <= 4 && (stages == 2 || stages == 4)) {
       set_tuned_launch(gp, sp, LsE, epi, DhopLaunch{th, spt, mode, stages});
       ++loaded;
     }

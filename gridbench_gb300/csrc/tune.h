@@ -12,4 +12,6 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
              double* norm2, bool fetch = true, const gbdw_field* cen = nullptr, double khop = 0.5);
 int check_operands(const gbdw_gauge* g, const gbdw_field* out, const gbdw_field* in, bool need_single_rhs);
 DhopParams make_params(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in);
+// form 4 (blocked site order) applies: FP32/FP16, Ls*nrhs = 16, periodic lattice, even extents
+bool blocked_ok(const gbdw_lattice* lat, const gbdw_field* in);
 }  // namespace gbdw

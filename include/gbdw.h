@@ -257,11 +257,12 @@ int gbdw_tune_load(const char* path);
 int gbdw_tune_save(const char* path);
 /* Writes the chosen shape for a field into cfg[4]: threads per CTA, slices per thread,
  * form (0 direct loads, 1 TMA-staged neighbour blocks with one ring per CTA, 2 the same with
- * one ring per warp, 3 the direct form specialised for FP32/FP16 with Ls*nrhs = 16) and stages of
+ * one ring per warp, 3 the direct form specialised for FP32/FP16 with Ls*nrhs = 16, 4 form 3 over 2x2x2x2
+ * site blocks on periodic lattices with even extents) and stages of
  * the staged forms. */
 int gbdw_tune_query(const gbdw_gauge* g, const gbdw_field* in, int cfg[4]);
 /* Pins the shape for fields like `in` (threads a multiple of 32 up to 256; slices per thread
- * 1, 2 or 4 dividing Ls*nrhs, at most 2 for F64; form 0..3; stages 2/4). */
+ * 1, 2 or 4 dividing Ls*nrhs, at most 2 for F64; form 0..4; stages 2/4). */
 int gbdw_tune_set(const gbdw_gauge* g, const gbdw_field* in, int threads, int spt, int form, int stages);
 
 /* ------------------------------------------------------------------ timing on the library stream */

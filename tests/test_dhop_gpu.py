@@ -241,3 +241,33 @@ def test_full_size_properties_16x16(gpu):
     Ds.axpby(-2.0, Da, 1.0)
     Ds.axpby(-1.0, Db, 1.0)
     assert np.sqrt(Ds.norm2() / Db.norm2()) < 1e-13
+
+
+@pytest.mark.parametrize("prec,tol", [(gb.F32, 1e-6), (gb.F16, 5e-3)])
+def test_blocked_site_order_form(gpu, prec, tol):
+    """Form 4: the Ls = 16 kernel with each CTA on a 2x2x2x2 block of sites (periodic lattice,
+    even extents): Dhop, DhopDag and M, against the oracle."""
+    dims = (4, 6, 2, 4)
+    c = make_case(dims, 16)
+    lat = gb.Lattice.periodic(dims, 16)
+    g = gb.Gauge(lat, c["U"], prec)
+    x = gb.Field(lat, prec).load(c["phi"])
+    y = gb.Field(lat, prec)
+    gb.tune_set(g, x, 128, 2, 4, 4)
+    assert tuple(gb.tune_query(g, x)) == (128, 2, 4, 4)
+    for dag in (0, 1):
+        gb.dhop(g, y, x, dag)
+        ref = oracle.dslash(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], 16, dag)
+        assert rel_err(y.numpy(), ref) < tol, dag
+        n2 = gb.dwf_m(g, y, x, 1.8, 0.01, dag, want_norm=True)
+        refm = oracle.dwf_m(c["U"], c["phi"], c["nbr"], c["nsite"], 16, 1.8, 0.01, dag)
+        out = y.numpy()
+        assert rel_err(out, refm) < tol, dag
+        assert abs(n2 - float(np.sum(out ** 2))) / n2 < 1e-5
+    # a table lattice has no extents: the form is refused
+    lt = gb.Lattice.from_table(c["nbr"], c["prm"], c["nsite"], 16)
+    gt = gb.Gauge(lt, c["U"], prec)
+    xt = gb.Field(lt, prec).load(c["phi"])
+    with pytest.raises(gb.GbdwError):
+        gb.tune_set(gt, xt, 128, 2, 4, 4)
+    gb.synchronize()
