@@ -186,9 +186,12 @@ class Field(_Handle):
         check(load().gbdw_field_export(self.h, rhs, _ptr(out), F64 if dtype == np.float64 else F32))
         return out
 
-    def export_into(self, out: np.ndarray, rhs: int = 0) -> np.ndarray:
-        """Writes right-hand side rhs into a preallocated float64/float32 array (e.g. pinned)."""
-        check(load().gbdw_field_export(self.h, rhs, _ptr(out), F64 if out.dtype == np.float64 else F32))
+    def export_into(self, out: np.ndarray, rhs: int = 0, sync: bool = True) -> np.ndarray:
+        """Writes right-hand side rhs into a preallocated float64/float32 array.  sync=False
+        only queues the work on the library stream (out must be page-locked, e.g. a
+        PinnedArray's array; complete with synchronize())."""
+        fn = load().gbdw_field_export if sync else load().gbdw_field_export_async
+        check(fn(self.h, rhs, _ptr(out), F64 if out.dtype == np.float64 else F32))
         return out
 
     def gaussian(self, seed: int, rhs: int = 0) -> "Field":
@@ -372,6 +375,36 @@ def tune_save(path: str):
 
 def tune_load(path: str):
     check(load().gbdw_tune_load(path.encode()))
+
+
+class Stream:
+    """A non-blocking CUDA stream of the library; `with s:` makes the library queue on it."""
+
+    def __init__(self):
+        self.h = C.c_void_p()
+        check(load().gbdw_stream_create(C.byref(self.h)))
+
+    def __enter__(self):
+        check(load().gbdw_set_stream(self.h))
+        return self
+
+    def __exit__(self, *exc):
+        load().gbdw_set_stream(None)
+
+    def synchronize(self):
+        with self:
+            synchronize()
+
+    def close(self):
+        if self.h and self.h.value:
+            load().gbdw_stream_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class PinnedArray:

@@ -52,6 +52,8 @@ PROTOTYPES = {
     "gbdw_synchronize": (_i, []),
     "gbdw_launch_count": (_u64, []),
     "gbdw_set_stream": (_i, [_vp]),
+    "gbdw_stream_create": (_i, [_pp]),
+    "gbdw_stream_destroy": (_i, [_vp]),
     "gbdw_dslash_kernel": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _u64, _u64, _vp, _i, _dp]),
     "gbdw_generate_gauge": (_i, [_vp, _i, _u64, _vp]),
     "gbdw_generate_fermion": (_i, [_vp, _i, _i, _u64, _vp]),
@@ -68,6 +70,7 @@ PROTOTYPES = {
     "gbdw_field_zero": (_i, [_vp]),
     "gbdw_field_import": (_i, [_vp, _i, _vp, _i]),
     "gbdw_field_export": (_i, [_vp, _i, _vp, _i]),
+    "gbdw_field_export_async": (_i, [_vp, _i, _vp, _i]),
     "gbdw_field_copy": (_i, [_vp, _vp]),
     "gbdw_field_gaussian": (_i, [_vp, _i, _u64]),
     "gbdw_gauge_random": (_i, [_pp, _vp, _i, _u64]),

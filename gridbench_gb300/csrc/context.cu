@@ -178,6 +178,26 @@ int gbdw_set_stream(void* s) {
   return GBDW_OK;
 }
 
+int gbdw_stream_create(void** s) {
+  if (!s) return GBDW_ERR_INVALID;
+  if (int st = ensure_device()) return st;
+  cudaStream_t x;
+  GBDW_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+  *s = (void*)x;
+  return GBDW_OK;
+}
+
+int gbdw_stream_destroy(void* s) {
+  if (!s) return GBDW_OK;
+  if (g_have_user_stream && g_user_stream == (cudaStream_t)s) {
+    g_have_user_stream = false;
+    g_user_stream = nullptr;
+  }
+  GBDW_CUDA(cudaStreamSynchronize((cudaStream_t)s));
+  GBDW_CUDA(cudaStreamDestroy((cudaStream_t)s));
+  return GBDW_OK;
+}
+
 int gbdw_timer_create(gbdw_timer** t) {
   if (!t) return GBDW_ERR_INVALID;
   if (int st = ensure_device()) return st;

@@ -19,6 +19,17 @@ bool is_device_ptr(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// Page-locked host memory the GPU can address directly (over NVLink-C2C on GB300): its device
+// address, or null.
+const void* host_mapped(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 // Makes `bytes` of src available on the device: returns src itself for device memory,
 // otherwise a copy in scratch slot `slot`.
 int stage_in(const void* src, size_t bytes, int slot, const void** dev) {
@@ -552,12 +563,16 @@ int gbdw_field_import(gbdw_field* f, int rhs, const void* src, int src_prec) {
   const gbdw_lattice* L = f->lat;
   const int64_t n5 = L->nsite * L->Ls;
   const size_t bytes = size_t(n5) * 12 * (src_prec == GBDW_F64 ? 16 : 8);
-  const void* dsrc = nullptr;
-  if (int st = stage_in(src, bytes, 5, &dsrc)) return st;
   const int t = 256;
   // site blocks: 4 warps per CTA, 24*Ls reals of shared memory per warp
   const size_t blk_smem = 4 * size_t(24) * L->Ls * (src_prec == GBDW_F64 ? 8 : 4);
-  if (L->nsimd == 1 && f->nrhs == 1 && blk_smem <= 48 * 1024 && (uintptr_t(dsrc) & 15) == 0) {
+  const bool blocks = L->nsimd == 1 && f->nrhs == 1 && blk_smem <= 48 * 1024;
+  // the site-block kernel reads page-locked host memory in place (coalesced, no staging copy)
+  const void* dsrc = blocks ? host_mapped(src) : nullptr;
+  if (!dsrc || (uintptr_t(dsrc) & 15) != 0) {
+    if (int st = stage_in(src, bytes, 5, &dsrc)) return st;
+  }
+  if (blocks && (uintptr_t(dsrc) & 15) == 0) {
     const unsigned nb = unsigned((L->nsite + 3) / 4);
 #define GBDW_IB(SRC, P) \
   k_import_blocks<SRC, P><<<nb, 128, blk_smem, stream()>>>((const SRC*)dsrc, L->nsite, L->Ls, f->d, f->norm, f->LsP)
@@ -591,7 +606,7 @@ int gbdw_field_import(gbdw_field* f, int rhs, const void* src, int src_prec) {
   return GBDW_OK;
 }
 
-int gbdw_field_export(const gbdw_field* f, int rhs, void* dst, int dst_prec) {
+static int field_export(const gbdw_field* f, int rhs, void* dst, int dst_prec, bool sync) {
   if (!f || !dst || rhs < 0 || rhs >= f->nrhs || (dst_prec != GBDW_F64 && dst_prec != GBDW_F32)) {
     set_error("gbdw_field_export: invalid arguments");
     return GBDW_ERR_INVALID;
@@ -599,18 +614,31 @@ int gbdw_field_export(const gbdw_field* f, int rhs, void* dst, int dst_prec) {
   const gbdw_lattice* L = f->lat;
   const int64_t n5 = L->nsite * L->Ls;
   const size_t bytes = size_t(n5) * 12 * (dst_prec == GBDW_F64 ? 16 : 8);
-  const bool dev = is_device_ptr(dst);
+  const int t = 256;
+  const size_t blk_smem = 4 * size_t(24) * L->Ls * (dst_prec == GBDW_F64 ? 8 : 4);
+  const bool blocks = L->nsimd == 1 && f->nrhs == 1 && blk_smem <= 48 * 1024;
+  bool dev = is_device_ptr(dst);
   void* ddst = dst;
+  if (!dev && blocks) {
+    // page-locked host memory: the site-block kernel writes it in place
+    void* m = const_cast<void*>(host_mapped(dst));
+    if (m && (uintptr_t(m) & 15) == 0) {
+      ddst = m;
+      dev = true;
+    }
+  }
   if (!dev) {
+    if (!sync) {
+      set_error("gbdw_field_export_async: the destination must be device or page-locked host memory");
+      return GBDW_ERR_INVALID;
+    }
     ddst = scratch(bytes, 6);
     if (!ddst) {
       set_error("staging buffer allocation failed");
       return GBDW_ERR_ALLOC;
     }
   }
-  const int t = 256;
-  const size_t blk_smem = 4 * size_t(24) * L->Ls * (dst_prec == GBDW_F64 ? 8 : 4);
-  if (L->nsimd == 1 && f->nrhs == 1 && blk_smem <= 48 * 1024 && (uintptr_t(ddst) & 15) == 0) {
+  if (blocks && (uintptr_t(ddst) & 15) == 0) {
     const unsigned nb = unsigned((L->nsite + 3) / 4);
 #define GBDW_EB(DST, P) \
   k_export_blocks<DST, P><<<nb, 128, blk_smem, stream()>>>(f->d, f->norm, L->nsite, L->Ls, (DST*)ddst, f->LsP)
@@ -640,11 +668,17 @@ int gbdw_field_export(const gbdw_field* f, int rhs, void* dst, int dst_prec) {
 #undef GBDW_SE
   }
   GBDW_LAUNCHED();
-  if (!dev) {
-    GBDW_CUDA(cudaMemcpyAsync(dst, ddst, bytes, cudaMemcpyDeviceToHost, stream()));
-    GBDW_CUDA(cudaStreamSynchronize(stream()));
-  }
+  if (!dev) GBDW_CUDA(cudaMemcpyAsync(dst, ddst, bytes, cudaMemcpyDeviceToHost, stream()));
+  if (sync) GBDW_CUDA(cudaStreamSynchronize(stream()));
   return GBDW_OK;
+}
+
+int gbdw_field_export(const gbdw_field* f, int rhs, void* dst, int dst_prec) {
+  return field_export(f, rhs, dst, dst_prec, true);
+}
+
+int gbdw_field_export_async(const gbdw_field* f, int rhs, void* dst, int dst_prec) {
+  return field_export(f, rhs, dst, dst_prec, false);
 }
 
 int gbdw_field_copy(gbdw_field* dst, const gbdw_field* src) {

@@ -271,3 +271,30 @@ def test_blocked_site_order_form(gpu, prec, tol):
     with pytest.raises(gb.GbdwError):
         gb.tune_set(gt, xt, 128, 2, 4, 4)
     gb.synchronize()
+
+
+@pytest.mark.parametrize("prec", [gb.F64, gb.F32, gb.F16])
+def test_pinned_host_import_export_in_place(gpu, prec):
+    """Page-locked host buffers are read and written in place by the conversion kernels
+    (synchronous and queued export), with the same result as the staged path from pageable
+    memory; a queued export into pageable memory is refused."""
+    dims, Ls = (4, 4, 2, 6), 8
+    c = make_case(dims, Ls)
+    lat = gb.Lattice.periodic(dims, Ls)
+    n = c["phi"].size
+    hin = gb.PinnedArray(n, np.float64)
+    hin.array[:] = c["phi"]
+    x_pinned = gb.Field(lat, prec).load(hin.array)
+    x_paged = gb.Field(lat, prec).load(np.array(c["phi"]))
+    ref = x_paged.numpy()
+    assert np.array_equal(x_pinned.numpy(), ref)
+    hout = gb.PinnedArray(n, np.float64)
+    x_pinned.export_into(hout.array)
+    assert np.array_equal(hout.array, ref)
+    hout.array[:] = 0.0
+    with gb.Stream() as s:
+        x_pinned.export_into(hout.array, sync=False)
+        gb.synchronize()
+    assert np.array_equal(hout.array, ref)
+    with pytest.raises(gb.GbdwError):
+        x_pinned.export_into(np.zeros(n), sync=False)
