@@ -5,6 +5,7 @@
 #include <cstring>
 #include <mutex>
 #include <atomic>
+#include <map>
 
 #include "common.cuh"
 
@@ -23,7 +24,14 @@ struct ScratchSlot {
   void* p = nullptr;
   size_t bytes = 0;
 };
-ScratchSlot g_scratch[8];
+// One table of scratch slots per stream the library queues on (its own stream, or each stream
+// given to gbdw_set_stream), so work queued on different streams never shares a buffer.
+struct SlotTable {
+  ScratchSlot s[8];
+};
+SlotTable g_scratch_own;
+std::map<cudaStream_t, SlotTable> g_scratch_user;
+SlotTable& slot_table() { return g_have_user_stream ? g_scratch_user[g_user_stream] : g_scratch_own; }
 double* g_pinned = nullptr;
 }  // namespace
 
@@ -82,7 +90,7 @@ cudaStream_t stream() { return g_have_user_stream ? g_user_stream : g_own_stream
 void count_launch(uint64_t n) { g_launches += n; }
 
 void* scratch(size_t bytes, int slot) {
-  ScratchSlot& s = g_scratch[slot];
+  ScratchSlot& s = slot_table().s[slot];
   if (s.bytes >= bytes && s.p) return s.p;
   if (s.p) {
     cudaStreamSynchronize(stream());
@@ -194,6 +202,12 @@ int gbdw_stream_destroy(void* s) {
     g_user_stream = nullptr;
   }
   GBDW_CUDA(cudaStreamSynchronize((cudaStream_t)s));
+  auto it = g_scratch_user.find((cudaStream_t)s);
+  if (it != g_scratch_user.end()) {
+    for (ScratchSlot& q : it->second.s)
+      if (q.p) cudaFree(q.p);
+    g_scratch_user.erase(it);
+  }
   GBDW_CUDA(cudaStreamDestroy((cudaStream_t)s));
   return GBDW_OK;
 }

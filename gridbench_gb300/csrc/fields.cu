@@ -19,19 +19,17 @@ bool is_device_ptr(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-// Page-locked host memory the GPU can address directly (over NVLink-C2C on GB300): its device
-// address, or null.
-const void* host_mapped(const void* p) {
+bool is_pinned_host(const void* p) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
-    return nullptr;
+    return false;
   }
-  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+  return a.type == cudaMemoryTypeHost;
 }
 
 // Makes `bytes` of src available on the device: returns src itself for device memory,
-// otherwise a copy in scratch slot `slot`.
+// otherwise a copy in scratch slot `slot` (a staging buffer of the current stream).
 int stage_in(const void* src, size_t bytes, int slot, const void** dev) {
   if (is_device_ptr(src)) {
     *dev = src;
@@ -567,11 +565,10 @@ int gbdw_field_import(gbdw_field* f, int rhs, const void* src, int src_prec) {
   // site blocks: 4 warps per CTA, 24*Ls reals of shared memory per warp
   const size_t blk_smem = 4 * size_t(24) * L->Ls * (src_prec == GBDW_F64 ? 8 : 4);
   const bool blocks = L->nsimd == 1 && f->nrhs == 1 && blk_smem <= 48 * 1024;
-  // the site-block kernel reads page-locked host memory in place (coalesced, no staging copy)
-  const void* dsrc = blocks ? host_mapped(src) : nullptr;
-  if (!dsrc || (uintptr_t(dsrc) & 15) != 0) {
-    if (int st = stage_in(src, bytes, 5, &dsrc)) return st;
-  }
+  // host memory goes through a copy engine into the stream's staging buffer: the copy needs
+  // no SMs, so copies of work queued on other streams overlap with it
+  const void* dsrc = nullptr;
+  if (int st = stage_in(src, bytes, 5, &dsrc)) return st;
   if (blocks && (uintptr_t(dsrc) & 15) == 0) {
     const unsigned nb = unsigned((L->nsite + 3) / 4);
 #define GBDW_IB(SRC, P) \
@@ -617,18 +614,10 @@ static int field_export(const gbdw_field* f, int rhs, void* dst, int dst_prec, b
   const int t = 256;
   const size_t blk_smem = 4 * size_t(24) * L->Ls * (dst_prec == GBDW_F64 ? 8 : 4);
   const bool blocks = L->nsimd == 1 && f->nrhs == 1 && blk_smem <= 48 * 1024;
-  bool dev = is_device_ptr(dst);
+  const bool dev = is_device_ptr(dst);
   void* ddst = dst;
-  if (!dev && blocks) {
-    // page-locked host memory: the site-block kernel writes it in place
-    void* m = const_cast<void*>(host_mapped(dst));
-    if (m && (uintptr_t(m) & 15) == 0) {
-      ddst = m;
-      dev = true;
-    }
-  }
   if (!dev) {
-    if (!sync) {
+    if (!sync && !is_pinned_host(dst)) {
       set_error("gbdw_field_export_async: the destination must be device or page-locked host memory");
       return GBDW_ERR_INVALID;
     }

@@ -58,7 +58,9 @@ int gbdw_device_available(void);        /* 1 if a CUDA device can be used, else 
 int gbdw_synchronize(void);             /* waits for the library stream */
 uint64_t gbdw_launch_count(void);       /* kernels this process launched through the library */
 int gbdw_set_stream(void* cuda_stream); /* NULL = the library's own non-blocking stream */
-/* a non-blocking CUDA stream owned by the caller (for gbdw_set_stream) */
+/* a non-blocking CUDA stream owned by the caller (for gbdw_set_stream).  Each stream the
+ * library queues on gets its own scratch and staging buffers (freed by gbdw_stream_destroy for
+ * streams made here, held until exit for others). */
 int gbdw_stream_create(void** cuda_stream);
 int gbdw_stream_destroy(void* cuda_stream);
 
@@ -129,9 +131,9 @@ int gbdw_field_zero(gbdw_field* f);
 int gbdw_field_import(gbdw_field* f, int rhs, const void* src, int src_prec);
 int gbdw_field_export(const gbdw_field* f, int rhs, void* dst, int dst_prec);
 /* As gbdw_field_export, but returns once the work is queued on the library stream (dst must be
- * device or page-locked host memory; complete with gbdw_synchronize).  With Nsimd = 1 and one
- * rhs, import from and export to page-locked host memory read / write it in place from the
- * conversion kernel (no staging copy). */
+ * device or page-locked host memory; complete with gbdw_synchronize).  Host transfers run on a
+ * copy engine through a staging buffer of the current stream, so imports and exports queued on
+ * two streams overlap (the host link is full duplex). */
 int gbdw_field_export_async(const gbdw_field* f, int rhs, void* dst, int dst_prec);
 /* dst = src with precision conversion (same lattice and nrhs). */
 int gbdw_field_copy(gbdw_field* dst, const gbdw_field* src);

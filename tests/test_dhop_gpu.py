@@ -274,10 +274,10 @@ def test_blocked_site_order_form(gpu, prec, tol):
 
 
 @pytest.mark.parametrize("prec", [gb.F64, gb.F32, gb.F16])
-def test_pinned_host_import_export_in_place(gpu, prec):
-    """Page-locked host buffers are read and written in place by the conversion kernels
-    (synchronous and queued export), with the same result as the staged path from pageable
-    memory; a queued export into pageable memory is refused."""
+def test_pinned_host_import_export_and_queued_export(gpu, prec):
+    """Page-locked host buffers through the synchronous and the queued export on a library
+    stream give the same result as pageable memory; a queued export into pageable memory is
+    refused."""
     dims, Ls = (4, 4, 2, 6), 8
     c = make_case(dims, Ls)
     lat = gb.Lattice.periodic(dims, Ls)
