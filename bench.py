@@ -406,7 +406,13 @@ def run_ours(args, D: Dist) -> dict | None:
     xA = gb.Field(lat, gb.F32).load(phiA)
     xB = gb.Field(lat, gb.F32).load(gb.generate_fermion(DIMS, LS, 1, (9, 10, 11, 12)))
     yA, yB = gb.Field(lat, gb.F32), gb.Field(lat, gb.F32)
-    cfg = gb.tune_dhop(g, yA, xA)
+    if args.tune_load:
+        gb.tune_load(args.tune_load)
+    else:
+        gb.tune_dhop(g, yA, xA)
+    if args.tune_save:
+        gb.tune_save(args.tune_save)
+    cfg = gb.tune_query(g, xA)
     pairs = [(yA, xA), (yB, xB)]
     clocks = Clocks()
     clocks.start()
@@ -600,6 +606,9 @@ def main(argv=None):
     ap.add_argument("--cg-max-iter", type=int, default=20000)
     ap.add_argument("--only", choices=sorted(ONLY), help="time one hopping-term workload only (for profiling)")
     ap.add_argument("--shape", help="with --only: threads,slices_per_thread,form,stages")
+    ap.add_argument("--tune-save", help="write the headline kernel's tuned shapes to this JSON file")
+    ap.add_argument("--tune-load", help="take the headline kernel's shapes from this JSON file instead of tuning "
+                                        "(a profiler serialises launches, which changes the tuner's ranking)")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
