@@ -70,3 +70,24 @@ def test_cpp_shim_header_compiles():
         r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), p],
                            capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
+
+
+def test_empty_and_oversize_inputs_are_rejected_without_a_device():
+    """Empty lattices, zero Ls and lattices beyond the 32-bit row indexing (nsite*Ls*12 < 2^31,
+    e.g. 64^4 x Ls=16) fail with GBDW_ERR_INVALID before any device work."""
+    L = gb.load()
+    h = C.c_void_p()
+    nbr = np.zeros(8, dtype=np.uint64)
+    assert L.gbdw_lattice_from_table(C.byref(h), 0, 4, 1, nbr.ctypes.data, None) == _native.ERR_INVALID
+    assert L.gbdw_lattice_from_table(C.byref(h), 1, 0, 1, nbr.ctypes.data, None) == _native.ERR_INVALID
+    assert L.gbdw_lattice_from_table(C.byref(h), 1, 4, 3, nbr.ctypes.data, None) == _native.ERR_INVALID
+    big = np.array([64, 64, 64, 64], dtype=np.int32)
+    assert L.gbdw_lattice_create(C.byref(h), C.c_void_p(big.ctypes.data), 16) == _native.ERR_INVALID
+    assert "too large" in L.gbdw_last_error().decode()
+    ok = np.array([48, 48, 48, 48], dtype=np.int32)  # 85M 5D sites at Ls=16 fits
+    st = L.gbdw_lattice_create(C.byref(h), C.c_void_p(ok.ctypes.data), 16)
+    assert st in (_native.OK, _native.ERR_NO_DEVICE)
+    if st == _native.OK:
+        L.gbdw_lattice_destroy(h)
+    assert L.gbdw_dslash_kernel(1, 1, 1, nbr.ctypes.data, nbr.ctypes.data, nbr.ctypes.data, nbr.ctypes.data, 1, 0,
+                                None, 0, None) == _native.ERR_INVALID
