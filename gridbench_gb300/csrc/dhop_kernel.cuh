@@ -75,15 +75,20 @@ __device__ __forceinline__ cpx<float> b2c(unsigned w) {
   const float2 f = __bfloat1622float2(h);
   return {f.x, f.y};
 }
+// conj(a b - c d) with each complex product as two packed FMAs on (re, im):
+// a b = a.r (b.r, b.i) + a.i (-b.i, b.r).
+__device__ __forceinline__ cpx<float> cross_conj(cpx<float> a, cpx<float> b, cpx<float> c, cpx<float> d) {
+  float2 t = __fmul2_rn(make_float2(a.r, a.r), make_float2(b.r, b.i));
+  t = __ffma2_rn(make_float2(a.i, a.i), make_float2(-b.i, b.r), t);
+  t = __ffma2_rn(make_float2(-c.r, -c.r), make_float2(d.r, d.i), t);
+  t = __ffma2_rn(make_float2(-c.i, -c.i), make_float2(-d.i, d.r), t);
+  return {t.x, -t.y};
+}
 __device__ __forceinline__ void third_row(cpx<float> (&u)[3][3]) {
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     const int c1 = (c + 1) % 3, c2 = (c + 2) % 3;
-    cpx<float> t = cmul(u[0][c1], u[1][c2]);
-    const cpx<float> q = cmul(u[0][c2], u[1][c1]);
-    t.r -= q.r;
-    t.i -= q.i;
-    u[2][c] = {t.r, -t.i};
+    u[2][c] = cross_conj(u[0][c1], u[1][c2], u[0][c2], u[1][c1]);
   }
 }
 
@@ -170,6 +175,23 @@ __device__ __forceinline__ cp2 cunit2(cp2 a) {
   else if constexpr (C == 2) return {neg2(a.i), a.r};
   else return {a.i, neg2(a.r)};
 }
+// acc += (c a) * n for a unit c (codes of LegSpin) and a per-slice factor n (nn = -n).
+template <int C>
+__device__ __forceinline__ void cacc2(cp2& acc, cp2 a, float2 n, float2 nn) {
+  if constexpr (C == 0) {
+    acc.r = __ffma2_rn(a.r, n, acc.r);
+    acc.i = __ffma2_rn(a.i, n, acc.i);
+  } else if constexpr (C == 1) {
+    acc.r = __ffma2_rn(a.r, nn, acc.r);
+    acc.i = __ffma2_rn(a.i, nn, acc.i);
+  } else if constexpr (C == 2) {  // i a = (-a.i, a.r)
+    acc.r = __ffma2_rn(a.i, nn, acc.r);
+    acc.i = __ffma2_rn(a.r, n, acc.i);
+  } else {  // -i a = (a.i, -a.r)
+    acc.r = __ffma2_rn(a.i, n, acc.r);
+    acc.i = __ffma2_rn(a.r, nn, acc.i);
+  }
+}
 // Row r of the link (one complex per colour, the same for both slices) times h.
 __device__ __forceinline__ cp2 su3_row2(const cpx<float> (&u)[3], const cp2 (&h)[3]) {
   cp2 o;
@@ -235,27 +257,35 @@ __device__ __forceinline__ void hop_leg_pairs(const cpx<float> (&u)[3][3], const
     }
   }
   if constexpr (PIN == GBDW_F16) {
+    // U h is linear in h: the neighbour's per-slice norm scales the products as they are
+    // accumulated (FFMA2 in place of FADD2) instead of every projected component
 #pragma unroll
     for (int q = 0; q < NP; ++q) {
       const float2 nr = ldv<SMEM>(reinterpret_cast<const float2*>(nrm) + q);
+      const float2 nn = neg2(nr);
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        h0[q][c] = {__fmul2_rn(h0[q][c].r, nr), __fmul2_rn(h0[q][c].i, nr)};
-        h1[q][c] = {__fmul2_rn(h1[q][c].r, nr), __fmul2_rn(h1[q][c].i, nr)};
+      for (int r = 0; r < 3; ++r) {
+        const cp2 u0 = su3_row2(u[r], h0[q]);
+        const cp2 u1 = su3_row2(u[r], h1[q]);
+        cacc2<0>(acc[q][0 * 3 + r], u0, nr, nn);
+        cacc2<0>(acc[q][1 * 3 + r], u1, nr, nn);
+        cacc2<conj_unit<S::C0>::v>(acc[q][S::A * 3 + r], u0, nr, nn);
+        cacc2<conj_unit<S::C1>::v>(acc[q][S::B * 3 + r], u1, nr, nn);
       }
     }
+  } else {
+#pragma unroll
+    for (int q = 0; q < NP; ++q)
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        const cp2 u0 = su3_row2(u[r], h0[q]);
+        const cp2 u1 = su3_row2(u[r], h1[q]);
+        acc[q][0 * 3 + r] = cadd2(acc[q][0 * 3 + r], u0);
+        acc[q][1 * 3 + r] = cadd2(acc[q][1 * 3 + r], u1);
+        acc[q][S::A * 3 + r] = cadd2(acc[q][S::A * 3 + r], cunit2<conj_unit<S::C0>::v>(u0));
+        acc[q][S::B * 3 + r] = cadd2(acc[q][S::B * 3 + r], cunit2<conj_unit<S::C1>::v>(u1));
+      }
   }
-#pragma unroll
-  for (int q = 0; q < NP; ++q)
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-      const cp2 u0 = su3_row2(u[r], h0[q]);
-      const cp2 u1 = su3_row2(u[r], h1[q]);
-      acc[q][0 * 3 + r] = cadd2(acc[q][0 * 3 + r], u0);
-      acc[q][1 * 3 + r] = cadd2(acc[q][1 * 3 + r], u1);
-      acc[q][S::A * 3 + r] = cadd2(acc[q][S::A * 3 + r], cunit2<conj_unit<S::C0>::v>(u0));
-      acc[q][S::B * 3 + r] = cadd2(acc[q][S::B * 3 + r], cunit2<conj_unit<S::C1>::v>(u1));
-    }
 }
 
 // One leg on N single slices (FP64, or N == 1).
