@@ -11,9 +11,12 @@ working set (476 MB) is well above the 129 MB L2 between consecutive steps.
 The JSON line carries: value (device-timed GFLOP/s, inputs resident in HBM), the HBM
 roofline of the kernel (algorithmic bytes 2*S + 8*G/(Ls*k) per 5D site), e2e (the same
 metric through the public API with the step's input copied from pinned host memory and the
-result copied back every step), the CPU baseline (the oracle port timed on the host cores),
-SM clocks sampled during the timed region, the number of kernels launched, and secondary
-workloads (FP64, DhopDag, FP16 storage, 12-RHS, mixed vs plain CG, batched persistent).
+result copied back every step; steps alternate over two library streams so one step's
+write-back overlaps the next step's input copy), the CPU baseline (the oracle port timed on
+the host cores), SM clocks sampled during the timed region, the number of kernels launched,
+and secondary workloads (FP64, DhopDag, FP16 storage, 12-RHS, batched persistent, and CG to a
+1e-10 true residual at 32^4 x Ls=16: plain vs mixed on M^dag M and through the even-odd Schur
+complement).
 
 --impl reference times the reference's algorithm on the host CPU (the oracle port of
 dslash_simple.h, all host threads) on the same workload; each step is a bounded sample of
