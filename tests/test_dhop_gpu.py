@@ -12,7 +12,7 @@ from conftest import GOLDEN, make_case, rel_err
 
 pytestmark = pytest.mark.gpu
 
-TOL = {gb.F64: 1e-12, gb.F32: 1e-6}  # relative to the FP64 oracle (spec bar for FP32)
+TOL = {gb.F64: 1e-12, gb.F32: 1e-6}  # relative to the FP64 oracle (1e-6: the FP32 target)
 
 
 def _run(c, prec, dag=0, nrhs=1):
