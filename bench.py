@@ -11,8 +11,8 @@ working set (476 MB) is well above the 129 MB L2 between consecutive steps.
 The JSON line carries: value (device-timed GFLOP/s, inputs resident in HBM), the HBM
 roofline of the kernel (algorithmic bytes 2*S + 8*G/(Ls*k) per 5D site), e2e (the same
 metric through the public API with the step's input copied from pinned host memory and the
-result copied back every step; steps alternate over two library streams so one step's
-write-back overlaps the next step's input copy), the CPU baseline (the oracle port timed on
+result copied back every step; steps rotate over three library streams so one step's
+write-back overlaps the next steps' input copies), the CPU baseline (the oracle port timed on
 the host cores), SM clocks sampled during the timed region, the number of kernels launched,
 and secondary workloads (FP64, DhopDag, FP16 storage, 12-RHS, batched persistent, and CG to a
 1e-10 true residual at 32^4 x Ls=16: plain vs mixed on M^dag M and through the even-odd Schur
@@ -437,27 +437,28 @@ def run_ours(args, D: Dist) -> dict | None:
     traffic = ncu_traffic("dhop_f32_16^4x16")
 
     # end to end through the public API: pinned host input -> device -> Dhop -> pinned host
-    # output, every step.  Steps alternate over two library streams with their own fields and
-    # host buffers, so one step's result write-back overlaps the next step's input read (the
+    # output, every step.  Steps rotate over three library streams with their own fields and
+    # host buffers, so one step's result write-back overlaps the next steps' input reads (the
     # host link is full duplex); each step still moves its whole input in and result out.
     n = V5 * 24
-    hins = [gb.PinnedArray(n, np.float32) for _ in range(2)]
-    houts = [gb.PinnedArray(n, np.float32) for _ in range(2)]
+    NS = 3  # streams: a stream's next input copy queues behind its own previous write-back
+    hins = [gb.PinnedArray(n, np.float32) for _ in range(NS)]
+    houts = [gb.PinnedArray(n, np.float32) for _ in range(NS)]
     for h in hins:
         h.array[:] = phiA
-    streams = [gb.Stream(), gb.Stream()]
-    epairs = [(xA, yA), (xB, yB)]
+    streams = [gb.Stream() for _ in range(NS)]
+    epairs = [(xA, yA), (xB, yB), (gb.Field(lat, gb.F32), gb.Field(lat, gb.F32))]
 
     def e2e_step(i):
-        k = i % 2
+        k = i % NS
         with streams[k]:
             x, y = epairs[k]
             x.load(hins[k].array)
             gb.dhop(g, y, x)
             y.export_into(houts[k].array, sync=False)
 
-    e2e_steps = max(4, min(args.steps, 200)) // 2 * 2
-    for i in range(4):
+    e2e_steps = max(2 * NS, min(args.steps, 300)) // NS * NS
+    for i in range(2 * NS):
         e2e_step(i)
     for st in streams:
         st.synchronize()
@@ -470,14 +471,14 @@ def run_ours(args, D: Dist) -> dict | None:
     te = D.max(time.perf_counter() - t0) / e2e_steps
     check_out = np.empty(n, np.float32)
     yA.export_into(check_out)
-    e2e_ok = bool(np.array_equal(check_out, houts[0].array) and np.array_equal(check_out, houts[1].array))
+    e2e_ok = bool(all(np.array_equal(check_out, h.array) for h in houts))
     for st in streams:
         st.close()
     e2e = {"value": round(D.world * flops_step / te / 1e9, 2), "unit": "GFLOP/s",
            "h2d_bytes_per_step": int(hins[0].array.nbytes), "d2h_bytes_per_step": int(houts[0].array.nbytes),
            "steps": e2e_steps, "ms_per_step": round(te * 1e3, 4), "results_match": e2e_ok,
            "path": "Field.load(pinned FP32 reference layout) -> dhop -> Field.export_into(pinned, async); "
-                   "steps alternate over two streams"}
+                   f"steps rotate over {NS} streams"}
 
     # relative error of this FP32 result against the FP64 kernel on the same input
     g64 = gb.Gauge(lat, U, gb.F64)
