@@ -188,3 +188,26 @@ def test_checkerboard_needs_even_extents(gpu):
     lat = gb.Lattice.periodic((4, 3, 4, 4), 4)
     with pytest.raises(gb.GbdwError):
         lat.checkerboard()
+
+
+@pytest.mark.parametrize("shape", [(128, 2, 0, 4), (64, 2, 3, 4), (128, 1, 1, 4), (64, 2, 2, 2), (128, 2, 4, 4)])
+def test_eo_hopping_in_every_launch_form(gpu, shape):
+    """The half-lattice hopping term through each launch form of the FP32 kernel at Ls = 16
+    (the blocked form falls back to the specialised direct one on a half lattice), and the
+    fused Schur step (Dhop_oe with the diagonal of another field) in the same forms."""
+    dims, Ls = (4, 4, 2, 4), 16
+    c, lat, g, le, lo, ge, go = setup(dims, Ls, gb.F32)
+    x = gb.Field(lat, gb.F32).load(c["phi"])
+    xo = gb.Field(lo, gb.F32).pick(x)
+    xe = gb.Field(le, gb.F32).pick(x)
+    gb.tune_set(g, x, *shape)
+    y = gb.Field(le, gb.F32)
+    for dag in (0, 1):
+        gb.dhop_eo(ge, y, xo, dag)
+        ref = oracle.dslash(c["U"], masked(c["phi"], dims, Ls, 1), c["nbr"], c["prm"], c["nsite"], Ls, dag)
+        assert rel_err(y.numpy(), halves(ref, dims, Ls)[0]) < 1e-6, (shape, dag)
+        # (M x)_e = D5 x_e - 1/2 Dhop_eo x_o
+        gb.dwf_meo(ge, y, xo, xe, M5, MF, dag)
+        refm = oracle.dwf_m(c["U"], c["phi"], c["nbr"], c["nsite"], Ls, M5, MF, dag)
+        assert rel_err(y.numpy(), halves(refm, dims, Ls)[0]) < 1e-6, (shape, dag)
+    gb.synchronize()
