@@ -569,6 +569,36 @@ ONLY = {  # name -> (dims, Ls, spinor precision, gauge precision, dag)
 }
 
 
+CG_ONLY = ("cg_full_plain", "cg_full_mixed16", "cg_eo_plain", "cg_eo_mixed16")
+
+
+def run_cg_only(args) -> dict:
+    """One CG solve (16^4 x Ls=16, tol 1e-10), nothing else: the command its launch list is
+    captured with."""
+    import gridbench_gb300 as gb
+    dims, Ls, M5, mf = (16, 16, 16, 16), 16, 1.8, 0.01
+    lat = gb.Lattice.periodic(dims, Ls)
+    g64, g32, g16 = (gb.Gauge(lat, None, p, seed=77) for p in (gb.F64, gb.F32, gb.F16))
+    b = gb.Field(lat, gb.F64).gaussian(78)
+    x = gb.Field(lat, gb.F64)
+    # the shapes the tuner picks on a GB300 for these extents, pinned (a profiler would reorder it)
+    gb.tune_set(g32, gb.Field(lat, gb.F32), 64, 2, 2, 2)
+    gb.tune_set(g16, gb.Field(lat, gb.F16), 64, 2, 3, 4)
+    if args.only.startswith("cg_eo"):
+        le, lo = lat.checkerboard()
+        G = [(g.checkerboard(le), g.checkerboard(lo)) for g in (g64, g32, g16)]
+        if args.only == "cg_eo_plain":
+            st = gb.cg_solve_eo(G[0], x, b, M5, mf, gb.CG_PLAIN, delta=1e-4, g32=G[1])
+        else:
+            st = gb.cg_solve_eo(G[0], x, b, M5, mf, gb.CG_MIXED, delta=1e-2, g32=G[1], gsloppy=G[2],
+                                sloppy_prec=gb.F16)
+    elif args.only == "cg_full_plain":
+        st = gb.cg_solve(g64, x, b, M5, mf, gb.CG_PLAIN, delta=1e-4, g32=g32)
+    else:
+        st = gb.cg_solve(g64, x, b, M5, mf, gb.CG_MIXED, delta=0.03, g32=g32, gsloppy=g16, sloppy_prec=gb.F16)
+    return {"workload": args.only, "lattice": list(dims), "Ls": Ls, **st}
+
+
 def run_only(args) -> dict:
     """One hopping-term workload, nothing else: the command profiles are captured with.
     --shape threads,slices,form,stages pins the launch shape (form 0 direct, 1 TMA-staged CTA
@@ -609,7 +639,8 @@ def main(argv=None):
     ap.add_argument("--ref-seconds", type=float, default=30.0)
     ap.add_argument("--cg-small", action="store_true", help="CG secondary on 16^4 x 16 instead of 32^4 x 16")
     ap.add_argument("--cg-max-iter", type=int, default=20000)
-    ap.add_argument("--only", choices=sorted(ONLY), help="time one hopping-term workload only (for profiling)")
+    ap.add_argument("--only", choices=sorted(ONLY) + list(CG_ONLY),
+                    help="one hopping-term workload, or one CG solve at 16^4 x 16, only (for profiling)")
     ap.add_argument("--shape", help="with --only: threads,slices_per_thread,form,stages")
     ap.add_argument("--tune-save", help="write the headline kernel's tuned shapes to this JSON file")
     ap.add_argument("--tune-load", help="take the headline kernel's shapes from this JSON file instead of tuning "
@@ -618,7 +649,7 @@ def main(argv=None):
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.only:
-        print(json.dumps(run_only(args)), flush=True)
+        print(json.dumps(run_cg_only(args) if args.only in CG_ONLY else run_only(args)), flush=True)
         return
     D = Dist()
     try:

@@ -122,14 +122,20 @@ struct conj_unit {
 };
 
 // ------------------------------------------------------------------ device reductions
-// Block-wide sum followed by a "last block finishes" pass over the per-block partials, so
-// the sum order is fixed (deterministic) and no second launch is needed.  partials holds
-// gridDim.x * W doubles, counter one unsigned that must be zero on entry and is left zero.
+// Block-wide sums, then "last block finishes" passes over the per-block partials, so the sum
+// order is fixed (deterministic) and no second launch is needed.
+//
+// grid_sum_flat: the last block sums all gridDim partials.  partials holds gridDim.x * W
+// doubles, counter one unsigned that must be zero on entry and is left zero.
+//
+// grid_sum: two levels, so no single block walks thousands of partials after everyone else
+// has finished: the last block of each group of kReduceGroup blocks sums its group (the sum
+// replaces the group's first partial), and the last group to finish sums the group sums.
+// counter holds 1 + ceil(gridDim.x / kReduceGroup) unsigned, zero on entry, left zero.
+constexpr unsigned kReduceGroup = 128;
+
 template <int W>
-__device__ __forceinline__ void grid_sum(double (&v)[W], double* partials, unsigned* counter,
-                                         double* result) {
-  __shared__ double sh[32][W];
-  __shared__ bool last;
+__device__ __forceinline__ void block_sum_to_thread0(double (&v)[W], double (&sh)[32][W]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int w = 0; w < W; ++w) {
@@ -145,8 +151,34 @@ __device__ __forceinline__ void grid_sum(double (&v)[W], double* partials, unsig
     for (int w = 0; w < W; ++w) {
       double x = 0.0;
       for (int k = 0; k < nw; ++k) x += sh[k][w];
-      partials[size_t(blockIdx.x) * W + w] = x;
+      v[w] = x;
     }
+  }
+}
+
+// Sum of partials[(first + k*stride)*W + w] for k < n, by the whole block, into thread 0's v.
+template <int W>
+__device__ __forceinline__ void block_sum_of(const double* partials, unsigned first, unsigned stride, unsigned n,
+                                             double (&v)[W], double (&sh)[32][W]) {
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    double x = 0.0;
+    for (unsigned k = threadIdx.x; k < n; k += blockDim.x)
+      x += __ldcg(&partials[size_t(first + k * stride) * W + w]);
+    v[w] = x;
+  }
+  block_sum_to_thread0<W>(v, sh);
+}
+
+template <int W>
+__device__ __forceinline__ void grid_sum_flat(double (&v)[W], double* partials, unsigned* counter,
+                                              double* result) {
+  __shared__ double sh[32][W];
+  __shared__ bool last;
+  block_sum_to_thread0<W>(v, sh);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int w = 0; w < W; ++w) partials[size_t(blockIdx.x) * W + w] = v[w];
     __threadfence();
     const unsigned prev = atomicAdd(counter, 1u);
     last = (prev == gridDim.x - 1);
@@ -154,25 +186,50 @@ __device__ __forceinline__ void grid_sum(double (&v)[W], double* partials, unsig
   __syncthreads();
   if (!last) return;
   __threadfence();
+  block_sum_of<W>(partials, 0, 1, gridDim.x, v, sh);
+  if (threadIdx.x == 0) {
 #pragma unroll
-  for (int w = 0; w < W; ++w) {
-    double x = 0.0;
-    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x)
-      x += __ldcg(&partials[size_t(b) * W + w]);
+    for (int w = 0; w < W; ++w) result[w] = v[w];
+    *counter = 0u;
+  }
+}
+
+template <int W>
+__device__ __forceinline__ void grid_sum(double (&v)[W], double* partials, unsigned* counter,
+                                         double* result) {
+  __shared__ double sh[32][W];
+  __shared__ bool last;
+  const unsigned g = blockIdx.x / kReduceGroup, g0 = g * kReduceGroup;
+  const unsigned ng = (gridDim.x + kReduceGroup - 1) / kReduceGroup;
+  const unsigned gsize = min(kReduceGroup, gridDim.x - g0);
+  block_sum_to_thread0<W>(v, sh);
+  if (threadIdx.x == 0) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    if (lane == 0) sh[warp][w] = x;
+    for (int w = 0; w < W; ++w) partials[size_t(blockIdx.x) * W + w] = v[w];
+    __threadfence();
+    const unsigned prev = atomicAdd(&counter[1 + g], 1u);
+    last = (prev == gsize - 1);
   }
   __syncthreads();
+  if (!last) return;
+  __threadfence();
+  block_sum_of<W>(partials, g0, 1, gsize, v, sh);  // this group, fixed order
   if (threadIdx.x == 0) {
-    const int nw = (blockDim.x + 31) >> 5;
 #pragma unroll
-    for (int w = 0; w < W; ++w) {
-      double x = 0.0;
-      for (int k = 0; k < nw; ++k) x += sh[k][w];
-      result[w] = x;
-    }
-    *counter = 0u;
+    for (int w = 0; w < W; ++w) partials[size_t(g0) * W + w] = v[w];
+    counter[1 + g] = 0u;
+    __threadfence();
+    const unsigned prev = atomicAdd(&counter[0], 1u);
+    last = (prev == ng - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  block_sum_of<W>(partials, 0, kReduceGroup, ng, v, sh);  // the group sums, fixed order
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int w = 0; w < W; ++w) result[w] = v[w];
+    counter[0] = 0u;
   }
 }
 

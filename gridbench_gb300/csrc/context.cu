@@ -27,7 +27,7 @@ struct ScratchSlot {
 // One table of scratch slots per stream the library queues on (its own stream, or each stream
 // given to gbdw_set_stream), so work queued on different streams never shares a buffer.
 struct SlotTable {
-  ScratchSlot s[8];
+  ScratchSlot s[12];
 };
 SlotTable g_scratch_own;
 std::map<cudaStream_t, SlotTable> g_scratch_user;
@@ -117,14 +117,16 @@ void* scratch(size_t bytes, int slot) {
 
 int reduce_scratch(int64_t nblocks, int width, Reduce* r) {
   void* part = scratch(size_t(nblocks) * size_t(width) * sizeof(double), 0);
-  // slot 1: [counter (unsigned, padded to 64 B)] [result doubles]
+  // slot 1: result doubles at +64 (the device error word lives at +2048)
   void* ctl = scratch(4096, 1);
-  if (!part || !ctl) {
+  // slot 8: the two-level reduction's counters, 1 + one per group of kReduceGroup blocks
+  void* cnt = scratch((size_t(1) + size_t((nblocks + kReduceGroup - 1) / kReduceGroup)) * sizeof(unsigned), 8);
+  if (!part || !ctl || !cnt) {
     set_error("reduction scratch allocation failed");
     return GBDW_ERR_ALLOC;
   }
   r->partials = (double*)part;
-  r->counter = (unsigned*)ctl;
+  r->counter = (unsigned*)cnt;
   r->result = (double*)((char*)ctl + 64);
   return GBDW_OK;
 }

@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(kNoAllocThreads) k_norm2_noalloc(const R* __re
     acc[0] += re * re + im * im;
   }
   unsigned* counter = reinterpret_cast<unsigned*>(scratch + kNoAllocMaxBlocks + 1);
-  grid_sum<1>(acc, scratch, counter, scratch + kNoAllocMaxBlocks);
+  grid_sum_flat<1>(acc, scratch, counter, scratch + kNoAllocMaxBlocks);
 }
 
 // Device address of the scratch array for the current device (looked up once per device).
