@@ -170,6 +170,20 @@ __device__ __forceinline__ void block_sum_of(const double* partials, unsigned fi
   block_sum_to_thread0<W>(v, sh);
 }
 
+// Block partials only: thread 0 of every block writes the block's sum to partials[blockIdx];
+// a separate one-CTA kernel (sum_partials) adds them up in a fixed order.  For grids of many
+// short blocks, where a fence and an atomic per block would hold every block until its
+// stores have landed.
+template <int W>
+__device__ __forceinline__ void block_partial(double (&v)[W], double* partials) {
+  __shared__ double sh[32][W];
+  block_sum_to_thread0<W>(v, sh);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int w = 0; w < W; ++w) partials[size_t(blockIdx.x) * W + w] = v[w];
+  }
+}
+
 template <int W>
 __device__ __forceinline__ void grid_sum_flat(double (&v)[W], double* partials, unsigned* counter,
                                               double* result) {
@@ -240,6 +254,8 @@ struct Reduce {
   double* result;
 };
 int reduce_scratch(int64_t nblocks, int width, Reduce* r);
+// result[0] = sum of partials[0..n) in a fixed order (one CTA, on the library stream)
+int sum_partials(const double* partials, int64_t n, double* result);
 int reduce_fetch(const Reduce& r, int width, double* host);
 
 }  // namespace gbdw

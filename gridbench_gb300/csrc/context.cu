@@ -131,6 +131,23 @@ int reduce_scratch(int64_t nblocks, int width, Reduce* r) {
   return GBDW_OK;
 }
 
+namespace {
+__global__ void __launch_bounds__(1024) k_sum_partials(const double* __restrict__ partials, int64_t n,
+                                                       double* result) {
+  double v[1] = {0.0};
+  for (int64_t k = threadIdx.x; k < n; k += blockDim.x) v[0] += partials[k];
+  __shared__ double sh[32][1];
+  block_sum_to_thread0<1>(v, sh);
+  if (threadIdx.x == 0) result[0] = v[0];
+}
+}  // namespace
+
+int sum_partials(const double* partials, int64_t n, double* result) {
+  k_sum_partials<<<1, 1024, 0, stream()>>>(partials, n, result);
+  GBDW_LAUNCHED();
+  return GBDW_OK;
+}
+
 unsigned* device_error_word() {
   void* ctl = scratch(4096, 1);
   return ctl ? (unsigned*)((char*)ctl + 2048) : nullptr;

@@ -116,7 +116,11 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
   else if (in->prec == GBDW_F32) st = launch_dhop_f32(p, dag, epi, L);
   else st = launch_dhop_f16(p, g->prec, dag, epi, L);
   if (st) return st;
-  if (norm2 && fetch) return reduce_fetch(red, 1, norm2);
+  if (norm2) {
+    // the kernel leaves one partial per CTA; one CTA sums them in a fixed order
+    if (int s2 = sum_partials(red.partials, blocks, red.result)) return s2;
+    if (fetch) return reduce_fetch(red, 1, norm2);
+  }
   return GBDW_OK;
 }
 

@@ -615,7 +615,7 @@ __global__ void __launch_bounds__(MINB > 0 ? MAXT : 256, MINB > 0 ? MINB : 1) k_
   }
   if (p.partials) {
     double v[1] = {POUT == GBDW_F64 ? dpart : double(part)};
-    grid_sum<1>(v, p.partials, p.counter, p.result);
+    block_partial<1>(v, p.partials);
   }
 }
 

@@ -173,9 +173,9 @@ __global__ void __launch_bounds__(256) k_dhop_tma(const DhopParams p, int NS) {
     if constexpr (POUT == GBDW_F64) dpart = sumsq<N>(out);
   }
   if (p.partials) {
-    // also reached after a timeout, so the grid reduction stays consistent
+    // also reached after a timeout, so every block's partial is written
     double v[1] = {POUT == GBDW_F64 ? dpart : double(part)};
-    grid_sum<1>(v, p.partials, p.counter, p.result);
+    block_partial<1>(v, p.partials);
   }
 }
 
@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(256) k_dhop_tmaw(const DhopParams p_) {
   }
   if (p.partials) {
     double v[1] = {POUT == GBDW_F64 ? dpart : double(part)};
-    grid_sum<1>(v, p.partials, p.counter, p.result);
+    block_partial<1>(v, p.partials);
   }
 }
 
