@@ -98,9 +98,10 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
   size_t smem = 0;
   const bool staged = L.mode == 1 || L.mode == 2;
   if (staged && !tma_shape(in->prec, in->LsE, L, &NS, &tthreads, &smem)) L.mode = 0;
+  // fall back before fixing the CTA size: the block count below must match the launch
+  if (L.mode == 4 && !blocked_ok(g->lat, in)) L.mode = 3;
   if (L.mode == 3 && (in->prec == GBDW_F64 || L.spt != 2 || in->LsE != 16 || in->LsP != 16)) L.mode = 0;
   if (L.mode == 3) L.threads = 64;
-  if (L.mode == 4 && !blocked_ok(g->lat, in)) L.mode = 3;
   if (L.mode == 4) L.threads = 128;
   const int64_t nthreads = p.nsite * (p.LsE / L.spt);
   const int64_t blocks = staged ? (p.nsite + NS - 1) / NS : (nthreads + L.threads - 1) / L.threads;

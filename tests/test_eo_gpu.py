@@ -210,4 +210,10 @@ def test_eo_hopping_in_every_launch_form(gpu, shape):
         gb.dwf_meo(ge, y, xo, xe, M5, MF, dag)
         refm = oracle.dwf_m(c["U"], c["phi"], c["nbr"], c["nsite"], Ls, M5, MF, dag)
         assert rel_err(y.numpy(), halves(refm, dims, Ls)[0]) < 1e-6, (shape, dag)
+        # the fused |out|^2 counts every CTA of the form actually launched (a half lattice
+        # runs the blocked form's fallback)
+        t1, t2, z = gb.Field(le, gb.F32), gb.Field(le, gb.F32), gb.Field(lo, gb.F32)
+        n2 = gb.dwf_mpc(go, ge, z, t1, t2, xo, M5, MF, dag, want_norm=True)
+        zz = z.numpy()
+        assert abs(n2 - float(np.sum(zz * zz))) / n2 < 1e-5, (shape, dag)
     gb.synchronize()
