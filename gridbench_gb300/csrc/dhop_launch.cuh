@@ -11,8 +11,12 @@ int go_direct(const DhopParams& p, DhopLaunch L) {
   const int64_t nthreads = p.nsite * (p.LsE / N);
   const unsigned blocks = unsigned((nthreads + L.threads - 1) / L.threads);
   if constexpr (PIN == GBDW_F32 && N == 2) {
-    if (p.LsE == 16 && p.LsP == 16) {
-      k_dhop<PIN, POUT, GP, DAG, N, EPI, 0, 16><<<blocks, L.threads, 0, stream()>>>(p);
+    // compile-time row strides for the extents of the benchmarked shapes: Ls = 16, and Ls = 12
+    // with one or 12 right-hand sides
+    if (p.LsE == p.LsP && (p.LsE == 16 || p.LsE == 12 || p.LsE == 144)) {
+      if (p.LsE == 16) k_dhop<PIN, POUT, GP, DAG, N, EPI, 0, 16><<<blocks, L.threads, 0, stream()>>>(p);
+      else if (p.LsE == 12) k_dhop<PIN, POUT, GP, DAG, N, EPI, 0, 12><<<blocks, L.threads, 0, stream()>>>(p);
+      else k_dhop<PIN, POUT, GP, DAG, N, EPI, 0, 144><<<blocks, L.threads, 0, stream()>>>(p);
       GBDW_LAUNCHED();
       return GBDW_OK;
     }
