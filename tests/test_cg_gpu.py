@@ -60,3 +60,27 @@ def test_cg_rejects_wrong_precisions(setup):
     x = gb.Field(lat, gb.F64)
     with pytest.raises(gb.GbdwError):
         gb.cg_solve(g64, x, b, M5, MF, gb.CG_MIXED, gsloppy=g32, sloppy_prec=gb.F16)
+
+
+def test_cg_mixed_with_bf16_links_and_initial_guess(setup):
+    """FP16 spinors with BF16 12-real links as the sloppy operator, and a non-zero initial
+    guess (the first true residual is then computed, not copied from b)."""
+    c, lat, g64, g32, g16, b, Ls = setup
+    gbf = gb.Gauge(lat, c["U"], gb.BF16)
+    x = gb.Field(lat, gb.F64).load(0.01 * c["phi"])
+    st = gb.cg_solve(g64, x, b, M5, MF, gb.CG_MIXED, tol=1e-10, max_iter=5000, delta=0.1, g32=g32, gsloppy=gbf,
+                     sloppy_prec=gb.F16)
+    assert st["true_residual"] <= 1e-10
+    assert _true_residual(c, x.numpy(), Ls) <= 2e-10
+
+
+@pytest.mark.parametrize("delta", [0.3, 1e-4])
+def test_cg_reliable_update_threshold_extremes(setup, delta):
+    """A frequent (0.3) and a rare (1e-4) reliable-update threshold both reach the target with
+    the FP32 sloppy operator; the rare one needs fewer updates."""
+    c, lat, g64, g32, g16, b, Ls = setup
+    x = gb.Field(lat, gb.F64)
+    st = gb.cg_solve(g64, x, b, M5, MF, gb.CG_MIXED, tol=1e-10, max_iter=5000, delta=delta, g32=g32, gsloppy=g32,
+                     sloppy_prec=gb.F32)
+    assert st["true_residual"] <= 1e-10 and _true_residual(c, x.numpy(), Ls) <= 2e-10
+    assert st["reliable_updates"] <= (3 if delta < 1e-3 else 40)
