@@ -83,4 +83,4 @@ def test_cg_reliable_update_threshold_extremes(setup, delta):
     st = gb.cg_solve(g64, x, b, M5, MF, gb.CG_MIXED, tol=1e-10, max_iter=5000, delta=delta, g32=g32, gsloppy=g32,
                      sloppy_prec=gb.F32)
     assert st["true_residual"] <= 1e-10 and _true_residual(c, x.numpy(), Ls) <= 2e-10
-    assert st["reliable_updates"] <= (3 if delta < 1e-3 else 40)
+    assert st["reliable_updates"] <= (4 if delta < 1e-3 else 40)
