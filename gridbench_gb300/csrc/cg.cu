@@ -38,11 +38,16 @@ struct Fields {
 
 // out = A in, and |M in|^2 (= <in, A in>) into pap when non-null.
 using Op = std::function<int(gbdw_field* out, const gbdw_field* in, double* pap)>;
+// One CG step's operator with the residual update fused into its last pass:
+//   r -= alpha A p with alpha = rr / <p, A p>; out = {<p, A p>, alpha, |r|^2}.  sink: a field of
+//   p's lattice and precision the passes may name as their output.
+using FusedOp = std::function<int(const gbdw_field* p, gbdw_field* sink, gbdw_field* r, double rr, double out[3])>;
 
 struct Problem {
   const gbdw_lattice* lat;  // lattice of x and b
   Op exact;                 // A on FP64 fields
   Op sloppy;                // A on fields of precision `op_prec`
+  FusedOp fused;            // when set (PLAIN and MIXED): A and the r update in one pass pair
   int op_prec;              // F64 (DOUBLE), F32 (PLAIN) or the sloppy precision (MIXED)
 };
 
@@ -116,17 +121,28 @@ int cg_core(const Problem& P, int mode, gbdw_field* x, const gbdw_field* b, cons
   int it = 0;
   int err = GBDW_OK;
   double rr_true = rr;
+  const bool fused = P.fused && mode != GBDW_CG_DOUBLE;
   while (!converged && it < prm->max_iter) {
-    double pap = 0.0;
-    TRY(P.sloppy(ap, pq ? pq : p, &pap));
+    double pap = 0.0, alpha = 0.0, rr_new = 0.0;
+    if (fused) {
+      // A p, alpha = rr / <p, A p> on the device, and r -= alpha A p in the last pass
+      double s[3];
+      TRY(P.fused(pq ? pq : p, ap, rs, rr, s));
+      pap = s[0];
+      alpha = s[1];
+      rr_new = s[2];
+    } else {
+      TRY(P.sloppy(ap, pq ? pq : p, &pap));
+    }
     if (!(pap > 0.0) || !std::isfinite(pap)) {
       set_error(std::string(who) + ": <p, A p> is not positive (operator or precision breakdown)");
       err = GBDW_ERR_DIVERGED;
       break;
     }
-    const double alpha = rr / pap;
-    double rr_new = 0.0;
-    TRY(blas_cg_r(alpha, rs, ap, &rr_new));
+    if (!fused) {
+      alpha = rr / pap;
+      TRY(blas_cg_r(alpha, rs, ap, &rr_new));
+    }
     ++it;
     if (!std::isfinite(rr_new)) {
       TRY(blas_axpby(alpha, p, 1.0, xs));
@@ -248,6 +264,10 @@ extern "C" int gbdw_cg_solve(const gbdw_gauge* g64, const gbdw_gauge* g32, const
   P.sloppy = [&](gbdw_field* out, const gbdw_field* in, double* pap) {
     return gbdw_dwf_mdagm(gop, out, tmps ? tmps : tmp64, in, M5, mf, pap);
   };
+  if (tmps)
+    P.fused = [&](const gbdw_field* in, gbdw_field*, gbdw_field* r, double rr, double out[3]) {
+      return mdagm_residual(gop, tmps, r, in, M5, mf, rr, out);
+    };
   return cg_core(P, mode, x, b, prm, stats, who);
 }
 
@@ -320,6 +340,10 @@ extern "C" int gbdw_cg_solve_eo(const gbdw_gauge* const g64[2], const gbdw_gauge
     if (op_prec == GBDW_F64) return mpcdagmpc(gpo, gqe, out, tp64, te, ue, in, M5, mf, pap);
     return mpcdagmpc(gpo, gqe, out, tps, tq1s, tq2s, in, M5, mf, pap);
   };
+  if (op_prec != GBDW_F64)
+    P.fused = [&](const gbdw_field* in, gbdw_field* sink, gbdw_field* r, double rr, double out[3]) {
+      return mpcdagmpc_residual(gpo, gqe, sink, tps, tq1s, tq2s, r, in, M5, mf, rr, out);
+    };
   gbdw_cg_stats S{};
   const int cst = cg_core(P, mode, xo, co, prm, &S, who);
   if (cst != GBDW_OK && cst != GBDW_ERR_NOT_CONVERGED && cst != GBDW_ERR_DIVERGED) return cst;

@@ -254,8 +254,13 @@ struct Reduce {
   double* result;
 };
 int reduce_scratch(int64_t nblocks, int width, Reduce* r);
-// result[0] = sum of partials[0..n) in a fixed order (one CTA, on the library stream)
-int sum_partials(const double* partials, int64_t n, double* result);
+// result[0] = sum of partials[0..n) in a fixed order (one CTA, on the library stream); with
+// alpha_out, also alpha_out[0] = num / result[0] (the CG step length, computed on the device)
+int sum_partials(const double* partials, int64_t n, double* result, double num = 0.0, double* alpha_out = nullptr);
+// three device doubles for one fused CG step: <p, A p>, alpha, |r|^2 after the update
+double* cg_scalars();
+// copies n <= 8 device doubles to the host (synchronising the library stream)
+int fetch_doubles(const double* dev, int n, double* host);
 int reduce_fetch(const Reduce& r, int width, double* host);
 
 }  // namespace gbdw

@@ -133,18 +133,30 @@ int reduce_scratch(int64_t nblocks, int width, Reduce* r) {
 
 namespace {
 __global__ void __launch_bounds__(1024) k_sum_partials(const double* __restrict__ partials, int64_t n,
-                                                       double* result) {
+                                                       double* result, double num, double* alpha_out) {
   double v[1] = {0.0};
   for (int64_t k = threadIdx.x; k < n; k += blockDim.x) v[0] += partials[k];
   __shared__ double sh[32][1];
   block_sum_to_thread0<1>(v, sh);
-  if (threadIdx.x == 0) result[0] = v[0];
+  if (threadIdx.x == 0) {
+    result[0] = v[0];
+    if (alpha_out) alpha_out[0] = num / v[0];
+  }
 }
 }  // namespace
 
-int sum_partials(const double* partials, int64_t n, double* result) {
-  k_sum_partials<<<1, 1024, 0, stream()>>>(partials, n, result);
+int sum_partials(const double* partials, int64_t n, double* result, double num, double* alpha_out) {
+  k_sum_partials<<<1, 1024, 0, stream()>>>(partials, n, result, num, alpha_out);
   GBDW_LAUNCHED();
+  return GBDW_OK;
+}
+
+double* cg_scalars() { return (double*)scratch(64, 9); }
+
+int fetch_doubles(const double* dev, int n, double* host) {
+  GBDW_CUDA(cudaMemcpyAsync(g_pinned, dev, size_t(n) * sizeof(double), cudaMemcpyDeviceToHost, stream()));
+  GBDW_CUDA(cudaStreamSynchronize(stream()));
+  for (int k = 0; k < n; ++k) host[k] = g_pinned[k];
   return GBDW_OK;
 }
 

@@ -71,9 +71,25 @@ DhopParams make_params(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* i
 }
 
 int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag, int epi, double a5, double mf,
-             double* norm2, bool fetch, const gbdw_field* cen, double khop) {
+             double* norm2, bool fetch, const gbdw_field* cen, double khop, const DhopExtra* ex) {
   if (int st = ensure_device()) return st;
+  const int tune_epi = epi;
+  if (ex && ex->r) {
+    // residual epilogue: the M pass's launch shape, r in place of the output
+    if (epi != 1 || !dag || ex->r->lat != out->lat || ex->r->nrhs != 1 || !ex->alpha ||
+        !(ex->r->prec == GBDW_F64 || ex->r->prec == GBDW_F32) || in->prec == GBDW_F64 ||
+        (ex->r->prec == GBDW_F64 && in->prec != GBDW_F32)) {
+      set_error("fused CG update: adjoint M pass, FP32/FP16 operator, FP32 or FP64 residual on its lattice");
+      return GBDW_ERR_INVALID;
+    }
+    epi = ex->r->prec == GBDW_F64 ? 3 : 2;
+  }
   DhopParams p = make_params(g, out, in);
+  if (ex && ex->r) {
+    p.r = ex->r->d;
+    p.rLsP = ex->r->LsP;
+    p.alpha = ex->alpha;
+  }
   p.a5 = a5;
   p.mf = mf;
   p.khop = khop;
@@ -92,7 +108,7 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
     set_error("device error word allocation failed");
     return GBDW_ERR_ALLOC;
   }
-  DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, epi);
+  DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, tune_epi);
   if (in->LsE % L.spt != 0) L.spt = 1;
   int NS = 0, tthreads = 0;
   size_t smem = 0;
@@ -106,7 +122,8 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
   const int64_t nthreads = p.nsite * (p.LsE / L.spt);
   const int64_t blocks = staged ? (p.nsite + NS - 1) / NS : (nthreads + L.threads - 1) / L.threads;
   Reduce red;
-  if (norm2) {
+  const bool reduce = norm2 || (ex && ex->sum_to);
+  if (reduce) {
     if (int st = reduce_scratch(blocks, 1, &red)) return st;
     p.partials = red.partials;
     p.counter = red.counter;
@@ -117,10 +134,11 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
   else if (in->prec == GBDW_F32) st = launch_dhop_f32(p, dag, epi, L);
   else st = launch_dhop_f16(p, g->prec, dag, epi, L);
   if (st) return st;
-  if (norm2) {
+  if (reduce) {
     // the kernel leaves one partial per CTA; one CTA sums them in a fixed order
-    if (int s2 = sum_partials(red.partials, blocks, red.result)) return s2;
-    if (fetch) return reduce_fetch(red, 1, norm2);
+    double* to = (ex && ex->sum_to) ? ex->sum_to : red.result;
+    if (int s2 = sum_partials(red.partials, blocks, to, ex ? ex->num : 0.0, ex ? ex->alpha_to : nullptr)) return s2;
+    if (norm2 && fetch) return ex && ex->sum_to ? fetch_doubles(to, 1, norm2) : reduce_fetch(red, 1, norm2);
   }
   return GBDW_OK;
 }
@@ -155,6 +173,27 @@ bool tma_shape(int prec, int LsE, DhopLaunch L, int* NS, int* threads, size_t* s
   *threads = round32(ns * Tps);
   *smem = sm;
   return true;
+}
+
+int mdagm_residual(const gbdw_gauge* g, gbdw_field* t, gbdw_field* r, const gbdw_field* p, double M5, double mf,
+                   double rr, double out[3]) {
+  if (int st = check_operands(g, t, p, true)) return st;
+  double* s = cg_scalars();
+  if (!s) {
+    set_error("CG scalar scratch allocation failed");
+    return GBDW_ERR_ALLOC;
+  }
+  DhopExtra e1;
+  e1.sum_to = s;
+  e1.num = rr;
+  e1.alpha_to = s + 1;
+  if (int st = run_dhop(g, t, p, 0, 1, 5.0 - M5, mf, nullptr, false, nullptr, 0.5, &e1)) return st;
+  DhopExtra e2;
+  e2.r = r;
+  e2.alpha = s + 1;
+  e2.sum_to = s + 2;
+  if (int st = run_dhop(g, t, t, 1, 1, 5.0 - M5, mf, nullptr, false, nullptr, 0.5, &e2)) return st;
+  return fetch_doubles(s, 3, out);
 }
 
 }  // namespace gbdw

@@ -417,6 +417,11 @@ struct DhopParams {
   const float* cen_norm = nullptr;
   double khop = 0.5;
   int dims[4] = {0, 0, 0, 0};  // periodic lattice extents (the blocked site order needs them)
+  // CG residual epilogues (EPI 2: FP32 r, EPI 3: FP64 r): r -= alpha * M(in) in place of
+  // storing M(in), |r|^2 into the partials; alpha is read from device memory.
+  void* r = nullptr;
+  int rLsP = 0;
+  const double* alpha = nullptr;
 };
 
 // Writes N slices of v[N][12] (slices e0.., norms for F16); returns the sum of squares of
@@ -548,6 +553,40 @@ __device__ __forceinline__ void dwf_epilogue(const DhopParams& p, int64_t site, 
   }
 }
 
+// ------------------------------------------------------------------ per-site finish
+// EPI 0: store Dhop(in); EPI 1: store M(in); EPI 2 / 3: r -= alpha M(in) with r FP32 / FP64
+// (the CG residual update fused into the operator's second pass; M(in) is not stored).
+// Returns |what was stored|^2 in part (FP32 outputs) or dpart (FP64 outputs and EPI 2/3).
+template <int PIN, int POUT, int DAG, int N, int EPI, class T>
+__device__ __forceinline__ void finish_site(const DhopParams& p, int64_t site, int s0, int LsE, int LsP,
+                                            cpx<T> (&v)[N][12], float& part, double& dpart) {
+  if constexpr (EPI >= 1) dwf_epilogue<PIN, DAG, N>(p, site, s0, v);
+  if constexpr (EPI >= 2) {
+    constexpr int RP = EPI == 2 ? GBDW_F32 : GBDW_F64;
+    using TR = typename Arith<RP>::T;
+    const TR al = TR(*p.alpha);
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      cpx<TR> rv[N];
+      Vec<RP, N>::load(p.r, site * 12 + k, s0, p.rLsP, rv);
+      TR ks = TR(0);
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        rv[j].r -= al * TR(v[j][k].r);
+        rv[j].i -= al * TR(v[j][k].i);
+        ks += rv[j].r * rv[j].r + rv[j].i * rv[j].i;
+      }
+      s += double(ks);
+      Vec<RP, N>::store(p.r, site * 12 + k, s0, p.rLsP, rv);
+    }
+    dpart = s;
+  } else {
+    part = store_spinor<POUT, N>(p.out, p.out_norm, site, s0, LsE, LsP, v);
+    if constexpr (POUT == GBDW_F64) dpart = sumsq<N>(v);
+  }
+}
+
 // ------------------------------------------------------------------ kernels
 // Hopping sum for one thread: site and first slice s0 of N consecutive slices.
 template <int PIN, int GP, int DAG, int N>
@@ -609,12 +648,10 @@ __global__ void __launch_bounds__(MINB > 0 ? MAXT : 256, MINB > 0 ? MINB : 1) k_
     }
     cpx<T> acc[N][12];
     dhop_thread<PIN, GP, DAG, N>(p, site, s0, acc);
-    if constexpr (EPI == 1) dwf_epilogue<PIN, DAG, N>(p, site, s0, acc);
-    part = store_spinor<POUT, N>(p.out, p.out_norm, site, s0, p.LsE, p.LsP, acc);
-    if constexpr (POUT == GBDW_F64) dpart = sumsq<N>(acc);
+    finish_site<PIN, POUT, DAG, N, EPI>(p, site, s0, p.LsE, p.LsP, acc, part, dpart);
   }
   if (p.partials) {
-    double v[1] = {POUT == GBDW_F64 ? dpart : double(part)};
+    double v[1] = {(POUT == GBDW_F64 || EPI >= 2) ? dpart : double(part)};
     block_partial<1>(v, p.partials);
   }
 }

@@ -111,8 +111,20 @@ int by_shape(const DhopParams& p, DhopLaunch L) {
   return GBDW_ERR_INVALID;
 }
 
+// epi 0 Dhop, 1 M; the CG residual epilogues exist for the adjoint pass only: 2 (FP32 r, FP32
+// and FP16 spinors) and 3 (FP64 r, FP32 spinors).
 template <int PIN, int POUT, int GP, int S1, int S2>
 int dispatch(const DhopParams& p, int dag, int epi, DhopLaunch L) {
+  if (epi >= 2) {
+    if constexpr (PIN == GBDW_F32 || PIN == GBDW_F16) {
+      if (dag && epi == 2) return by_shape<PIN, POUT, GP, 1, 2, S1, S2>(p, L);
+    }
+    if constexpr (PIN == GBDW_F32) {
+      if (dag && epi == 3) return by_shape<PIN, POUT, GP, 1, 3, S1, S2>(p, L);
+    }
+    set_error("hopping kernel: residual epilogue not compiled for this precision / direction");
+    return GBDW_ERR_INVALID;
+  }
   if (dag) return epi ? by_shape<PIN, POUT, GP, 1, 1, S1, S2>(p, L) : by_shape<PIN, POUT, GP, 1, 0, S1, S2>(p, L);
   return epi ? by_shape<PIN, POUT, GP, 0, 1, S1, S2>(p, L) : by_shape<PIN, POUT, GP, 0, 0, S1, S2>(p, L);
 }

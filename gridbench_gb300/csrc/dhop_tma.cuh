@@ -168,13 +168,11 @@ __global__ void __launch_bounds__(256) k_dhop_tma(const DhopParams p, int NS) {
     const int64_t site = site0 + sl;
     cpx<T> out[N][12];
     acc.unpack(out);
-    if constexpr (EPI == 1) dwf_epilogue<PIN, DAG, N>(p, site, s0, out);
-    part = store_spinor<POUT, N>(p.out, p.out_norm, site, s0, LsE, LsP, out);
-    if constexpr (POUT == GBDW_F64) dpart = sumsq<N>(out);
+    finish_site<PIN, POUT, DAG, N, EPI>(p, site, s0, LsE, LsP, out, part, dpart);
   }
   if (p.partials) {
     // also reached after a timeout, so every block's partial is written
-    double v[1] = {POUT == GBDW_F64 ? dpart : double(part)};
+    double v[1] = {(POUT == GBDW_F64 || EPI >= 2) ? dpart : double(part)};
     block_partial<1>(v, p.partials);
   }
 }
@@ -295,12 +293,10 @@ __global__ void __launch_bounds__(256) k_dhop_tmaw(const DhopParams p_) {
     const int64_t site = site0 + sl;
     cpx<T> out[N][12];
     acc.unpack(out);
-    if constexpr (EPI == 1) dwf_epilogue<PIN, DAG, N>(p, site, s0, out);
-    part = store_spinor<POUT, N>(p.out, p.out_norm, site, s0, LsE, LsP, out);
-    if constexpr (POUT == GBDW_F64) dpart = sumsq<N>(out);
+    finish_site<PIN, POUT, DAG, N, EPI>(p, site, s0, LsE, LsP, out, part, dpart);
   }
   if (p.partials) {
-    double v[1] = {POUT == GBDW_F64 ? dpart : double(part)};
+    double v[1] = {(POUT == GBDW_F64 || EPI >= 2) ? dpart : double(part)};
     block_partial<1>(v, p.partials);
   }
 }

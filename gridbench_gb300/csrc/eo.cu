@@ -264,13 +264,13 @@ int check_eo(const gbdw_gauge* g, const gbdw_field* out, const gbdw_field* in) {
 }
 
 int hop_eo(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag, const gbdw_field* cen, double M5,
-           double mf, double khop, double* norm2, bool fetch) {
+           double mf, double khop, double* norm2, bool fetch, const DhopExtra* ex) {
   if (int st = check_eo(g, out, in)) return st;
   if (cen && (cen->lat != out->lat || cen->prec != in->prec || cen->nrhs != 1 || in->nrhs != 1 || cen == out)) {
     set_error("even-odd operator: the diagonal field lives on the output half, same precision, single rhs");
     return GBDW_ERR_INVALID;
   }
-  return run_dhop(g, out, in, dag ? 1 : 0, cen ? 1 : 0, 5.0 - M5, mf, norm2, fetch, cen, khop);
+  return run_dhop(g, out, in, dag ? 1 : 0, cen ? 1 : 0, 5.0 - M5, mf, norm2, fetch, cen, khop, ex);
 }
 
 int mpc(const gbdw_gauge* gp, const gbdw_gauge* gq, gbdw_field* out, gbdw_field* tq1, gbdw_field* tq2,
@@ -302,6 +302,36 @@ int mpcdagmpc(const gbdw_gauge* gp, const gbdw_gauge* gq, gbdw_field* out, gbdw_
     return reduce_fetch(red, 1, pap);
   }
   return GBDW_OK;
+}
+
+int mpcdagmpc_residual(const gbdw_gauge* gp, const gbdw_gauge* gq, gbdw_field* sink, gbdw_field* tp, gbdw_field* tq1,
+                       gbdw_field* tq2, gbdw_field* r, const gbdw_field* in, double M5, double mf, double rr,
+                       double out[3]) {
+  if (!gp || !gq || gq->lat != gp->lat->partner || !tp || !tq1 || !tq2 || !sink || tp == in || sink == tp ||
+      sink == in) {
+    set_error("fused Schur step: partner gauge halves, distinct temporaries");
+    return GBDW_ERR_INVALID;
+  }
+  double* s = cg_scalars();
+  if (!s) {
+    set_error("CG scalar scratch allocation failed");
+    return GBDW_ERR_ALLOC;
+  }
+  DhopExtra e1;
+  e1.sum_to = s;
+  e1.num = rr;
+  e1.alpha_to = s + 1;
+  if (int st = hop_eo(gq, tq1, in, 0, nullptr, M5, mf, 0.5, nullptr, true)) return st;
+  if (int st = m5inv(tq2, tq1, M5, mf, 0)) return st;
+  if (int st = hop_eo(gp, tp, tq2, 0, in, M5, mf, 0.25, nullptr, false, &e1)) return st;
+  DhopExtra e2;
+  e2.r = r;
+  e2.alpha = s + 1;
+  e2.sum_to = s + 2;
+  if (int st = hop_eo(gq, tq1, tp, 1, nullptr, M5, mf, 0.5, nullptr, true)) return st;
+  if (int st = m5inv(tq2, tq1, M5, mf, 1)) return st;
+  if (int st = hop_eo(gp, sink, tq2, 1, tp, M5, mf, 0.25, nullptr, false, &e2)) return st;
+  return fetch_doubles(s, 3, out);
 }
 
 int field_pick(gbdw_field* half, const gbdw_field* full) {

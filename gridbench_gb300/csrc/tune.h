@@ -7,9 +7,23 @@ namespace gbdw {
 DhopLaunch tuned_launch(int gprec, int sprec, int LsE, int epi);
 DhopLaunch default_launch(int gprec, int sprec, int LsE, int epi);
 void set_tuned_launch(int gprec, int sprec, int LsE, int epi, DhopLaunch L);
+// Optional parts of a hopping launch used by the fused CG step.
+struct DhopExtra {
+  gbdw_field* r = nullptr;          // with epi 1: r -= (*alpha) M(in) instead of storing M(in)
+  const double* alpha = nullptr;    // device
+  double* sum_to = nullptr;         // device: where the fused |.|^2 goes (default: the reduce result)
+  double num = 0.0;                 // with alpha_to: alpha_to = num / sum
+  double* alpha_to = nullptr;       // device
+};
 // cen / khop: the M epilogue's diagonal field (default: in) and hopping coefficient (1/2)
 int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag, int epi, double a5, double mf,
-             double* norm2, bool fetch = true, const gbdw_field* cen = nullptr, double khop = 0.5);
+             double* norm2, bool fetch = true, const gbdw_field* cen = nullptr, double khop = 0.5,
+             const DhopExtra* ex = nullptr);
+// The two passes of M^dag M with the CG update of the second fused in:
+//   t = M p, s[0] = |t|^2, s[1] = alpha = rr / s[0], r -= alpha M^dag t, s[2] = |r|^2
+// (s = cg_scalars(), fetched into out[3] with one synchronisation).
+int mdagm_residual(const gbdw_gauge* g, gbdw_field* t, gbdw_field* r, const gbdw_field* p, double M5, double mf,
+                   double rr, double out[3]);
 int check_operands(const gbdw_gauge* g, const gbdw_field* out, const gbdw_field* in, bool need_single_rhs);
 DhopParams make_params(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in);
 // form 4 (blocked site order) applies: FP32/FP16, Ls*nrhs = 16, periodic lattice, even extents
