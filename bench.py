@@ -214,6 +214,34 @@ def rel_to(gb, lat, a, b) -> float:
     return float(np.sqrt(d.norm2() / bb.norm2()))
 
 
+def measured_fp64_peak() -> dict | None:
+    """FP64 throughput of the GPU, measured here: a cuBLAS DGEMM (8192^3, through torch, which
+    is only plumbing for this one number), best of 3 with CUDA events.  The FP64 hopping kernel
+    is FP64-pipe bound, so it is reported against this as well as against HBM."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return None
+        n = 8192
+        a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+        b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+        torch.matmul(a, b)
+        torch.cuda.synchronize()
+        best = 1e30
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1) / 1e3)
+        del a, b
+        torch.cuda.empty_cache()
+        return {"value": round(2.0 * n ** 3 / best / 1e12, 3), "unit": "TFLOP/s", "how": "cuBLAS DGEMM 8192^3"}
+    except Exception:
+        return None
+
+
 def secondary(gb, args, peak) -> dict:
     out = {}
     lat = gb.Lattice.periodic(DIMS, LS)
@@ -243,6 +271,10 @@ def secondary(gb, args, peak) -> dict:
                "launch": list(gb.tune_query(g, x))}
         if sp == 0:
             rec["fp64_tflops"] = round(FLOP_PER_SITE * V5 / t / 1e12, 3)
+            fp64_peak = measured_fp64_peak()
+            if fp64_peak:
+                rec["fp64_peak_tflops"] = fp64_peak
+                rec["fp64_frac"] = round(rec["fp64_tflops"] / fp64_peak["value"], 3)
         out[name] = rec
     del g64, g32, g16, x64, y64, x32, y32, x16, y16, lat
     if not args.quick:
