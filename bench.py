@@ -276,6 +276,31 @@ def secondary(gb, args, peak) -> dict:
                 rec["fp64_peak_tflops"] = fp64_peak
                 rec["fp64_frac"] = round(rec["fp64_tflops"] / fp64_peak["value"], 3)
         out[name] = rec
+    # even-odd: the hopping term between half lattices and the closed-form D5^-1 (FP32)
+    le, lo = lat.checkerboard()
+    ge = g32.checkerboard(le)
+    xo = gb.Field(lo, gb.F32).pick(x32)
+    ye, ze = gb.Field(le, gb.F32), gb.Field(le, gb.F32)
+    gb.tune_dhop(g32, y32, x32)
+    for _ in range(5):
+        gb.dhop_eo(ge, ye, xo)
+    gb.synchronize()
+    tm = gb.Timer()
+    tm.start()
+    for _ in range(steps):
+        gb.dhop_eo(ge, ye, xo)
+    t = tm.stop() / steps / 1e3
+    gb.dwf_m5inv(ze, ye, 1.8, 0.01)
+    gb.synchronize()
+    tm.start()
+    for _ in range(steps):
+        gb.dwf_m5inv(ze, ye, 1.8, 0.01)
+    t5 = tm.stop() / steps / 1e3
+    out["dhop_eo_f32_16^4x16"] = {
+        "gflops": round(FLOP_PER_SITE * V5 / 2 / t / 1e9, 1), "ms": round(t * 1e3, 4),
+        "hbm_frac": round(algo_bytes(1, 1, LS) * V5 / 2 / t / 1e9 / peak, 3), "launch": list(gb.tune_query(g32, x32)),
+        "m5inv_ms": round(t5 * 1e3, 4), "m5inv_hbm_frac": round(2 * 96 * V5 / 2 / t5 / 1e9 / peak, 3)}
+    del ge, xo, ye, ze, le, lo
     del g64, g32, g16, x64, y64, x32, y32, x16, y16, lat
     if not args.quick:
         out["multi_rhs_24^4x12_k12"] = bench_mrhs(gb, peak)
