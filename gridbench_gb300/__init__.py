@@ -19,7 +19,8 @@ from ._native import (BF16, CG_DOUBLE, CG_MIXED, CG_PLAIN, F16, F32, F64, CGPara
 __all__ = ["F64", "F32", "F16", "BF16", "CG_PLAIN", "CG_MIXED", "CG_DOUBLE", "GbdwError", "load",
            "device_available", "launch_count", "synchronize", "seed_from_ints", "generate_gauge",
            "generate_fermion", "generate_table", "Lattice", "Gauge", "Field", "dhop", "dwf_m", "dwf_mdagm",
-           "cg_solve", "Batch", "dslash_kernel", "Timer", "flush_l2"]
+           "cg_solve", "Batch", "dslash_kernel", "Timer", "flush_l2", "m5d", "m5d_inv", "mobius_mooee",
+           "mobius_mooee_inv", "mobius_m", "mobius_meooe", "mobius_mpc"]
 
 _DT = {F64: np.float64, F32: np.float32}
 
@@ -316,6 +317,58 @@ def cg_solve_eo(g64: Sequence[Gauge], x: Field, b: Field, M5: float, mf: float, 
     check(status)
     return {"iterations": st.iterations, "reliable_updates": st.reliable_updates,
             "true_residual": st.true_residual, "seconds": st.seconds, "final_rr": st.final_rr}
+
+
+# ------------------------------------------------------------------ Mobius / Cayley 5D operators
+def _coef(a, Ls: int):
+    v = np.ascontiguousarray(np.broadcast_to(np.asarray(a, dtype=np.float64), (Ls,)))
+    return v, v.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def m5d(out: Field, inp: Field, lower, diag, upper, dag: int = 0) -> None:
+    """(A psi)(s) = diag[s] psi(s) + upper[s] P- psi(s+1) + lower[s] P+ psi(s-1), s +- 1 mod Ls;
+    dag: the exact adjoint of the same A.  Coefficients: scalars or Ls values."""
+    Ls = inp.lat.info()["Ls"]
+    (lo, plo), (di, pdi), (up, pup) = _coef(lower, Ls), _coef(diag, Ls), _coef(upper, Ls)
+    check(load().gbdw_m5d(out.h, inp.h, plo, pdi, pup, int(dag)))
+
+
+def m5d_inv(out: Field, inp: Field, lower, diag, upper, dag: int = 0) -> None:
+    Ls = inp.lat.info()["Ls"]
+    (lo, plo), (di, pdi), (up, pup) = _coef(lower, Ls), _coef(diag, Ls), _coef(upper, Ls)
+    check(load().gbdw_m5d_inv(out.h, inp.h, plo, pdi, pup, int(dag)))
+
+
+def mobius_mooee(out: Field, inp: Field, b: float, c: float, M5: float, mf: float, dag: int = 0) -> None:
+    check(load().gbdw_mobius_mooee(out.h, inp.h, b, c, M5, mf, int(dag)))
+
+
+def mobius_mooee_inv(out: Field, inp: Field, b: float, c: float, M5: float, mf: float, dag: int = 0) -> None:
+    check(load().gbdw_mobius_mooee_inv(out.h, inp.h, b, c, M5, mf, int(dag)))
+
+
+def mobius_m(g: Gauge, out: Field, tmp: Field, inp: Field, b: float, c: float, M5: float, mf: float,
+             dag: int = 0, want_norm: bool = False):
+    """Mobius domain-wall M (M^dag for dag) on a full lattice: M = Mooee - 1/2 Dhop A(b, c)."""
+    v = C.c_double()
+    check(load().gbdw_mobius_m(g.h, out.h, tmp.h, inp.h, b, c, M5, mf, int(dag),
+                               C.byref(v) if want_norm else None))
+    return v.value if want_norm else None
+
+
+def mobius_meooe(g: Gauge, out: Field, tmp: Field, inp: Field, b: float, c: float, mf: float,
+                 dag: int = 0) -> None:
+    """Even-odd hopping block on g's half lattice (inp on the partner half)."""
+    check(load().gbdw_mobius_meooe(g.h, out.h, tmp.h, inp.h, b, c, mf, int(dag)))
+
+
+def mobius_mpc(gp: Gauge, gq: Gauge, out: Field, tp: Field, tq1: Field, tq2: Field, inp: Field, b: float,
+               c: float, M5: float, mf: float, dag: int = 0, want_norm: bool = False):
+    """Schur operator Mpc = Mooee - Meooe_pq Mooee^-1 Meooe_qp on gp's half lattice."""
+    v = C.c_double()
+    check(load().gbdw_mobius_mpc(gp.h, gq.h, out.h, tp.h, tq1.h, tq2.h, inp.h, b, c, M5, mf, int(dag),
+                                 C.byref(v) if want_norm else None))
+    return v.value if want_norm else None
 
 
 def cg_solve(g64: Gauge, x: Field, b: Field, M5: float, mf: float, mode: int, tol: float = 1e-10,

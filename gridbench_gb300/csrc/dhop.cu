@@ -93,6 +93,7 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
   p.a5 = a5;
   p.mf = mf;
   p.khop = khop;
+  if (ex) p.c5 = ex->c5;
   if (cen) {
     p.cen = cen->d;
     p.cen_norm = cen->norm;

@@ -416,6 +416,9 @@ struct DhopParams {
   const void* cen = nullptr;
   const float* cen_norm = nullptr;
   double khop = 0.5;
+  // coefficient of the 5th-dimension hopping part of the epilogue (1 for Shamir; the Mobius
+  // operator's diagonal block carries 1 - c (4 - M5) there)
+  double c5 = 1.0;
   int dims[4] = {0, 0, 0, 0};  // periodic lattice extents (the blocked site order needs them)
   // CG residual epilogues (EPI 2: FP32 r, EPI 3: FP64 r): r -= alpha * M(in) in place of
   // storing M(in), |r|^2 into the partials; alpha is read from device memory.
@@ -533,7 +536,7 @@ __device__ __forceinline__ void dwf_epilogue(const DhopParams& p, int64_t site, 
     nlo *= __ldg(cnorm + site * Ls + slo);
     nhi *= __ldg(cnorm + site * Ls + shi);
   }
-  const T a5 = T(p.a5), kh = T(p.khop);
+  const T a5 = T(p.a5), kh = T(p.khop), c5 = T(p.c5);
 #pragma unroll
   for (int j = 0; j < N; ++j) {
 #pragma unroll
@@ -544,11 +547,11 @@ __device__ __forceinline__ void dwf_epilogue(const DhopParams& p, int64_t site, 
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
       const cpx<T> m = (j == 0) ? cpx<T>{lo[k].r * nlo, lo[k].i * nlo} : cen[j - 1 < 0 ? 0 : j - 1][LO0 * 3 + k];
-      acc[j][LO0 * 3 + k].r -= m.r;
-      acc[j][LO0 * 3 + k].i -= m.i;
+      acc[j][LO0 * 3 + k].r -= c5 * m.r;
+      acc[j][LO0 * 3 + k].i -= c5 * m.i;
       const cpx<T> q = (j == N - 1) ? cpx<T>{hi[k].r * nhi, hi[k].i * nhi} : cen[j + 1 >= N ? N - 1 : j + 1][HI0 * 3 + k];
-      acc[j][HI0 * 3 + k].r -= q.r;
-      acc[j][HI0 * 3 + k].i -= q.i;
+      acc[j][HI0 * 3 + k].r -= c5 * q.r;
+      acc[j][HI0 * 3 + k].i -= c5 * q.i;
     }
   }
 }

@@ -14,6 +14,7 @@ struct DhopExtra {
   double* sum_to = nullptr;         // device: where the fused |.|^2 goes (default: the reduce result)
   double num = 0.0;                 // with alpha_to: alpha_to = num / sum
   double* alpha_to = nullptr;       // device
+  double c5 = 1.0;                  // the epilogue's 5th-dimension hopping coefficient
 };
 // cen / khop: the M epilogue's diagonal field (default: in) and hopping coefficient (1/2)
 int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag, int epi, double a5, double mf,

@@ -228,6 +228,44 @@ int gbdw_cg_solve_eo(const gbdw_gauge* const g_double[2], const gbdw_gauge* cons
                      const gbdw_gauge* const g_sloppy[2], gbdw_field* x, const gbdw_field* b,
                      double M5, double mf, int mode, const gbdw_cg_params* prm, gbdw_cg_stats* stats);
 
+/* ------------------------------------------------------------------ Mobius / Cayley 5D operators
+ * No counterpart in GridBench: the 5th-dimension operators Grid's CayleyFermion5D builds
+ * around the hopping term (M5D, M5Ddag, Mooee, MooeeInv, Meooe), for Mobius domain-wall
+ * fermions (Brower, Neff, Orginos, arXiv:1206.5214).  A cyclic 5th-dimension operator with
+ * per-slice real coefficients (arrays of Ls entries):
+ *   (A psi)(s) = diag[s] psi(s) + upper[s] P- psi(s+1) + lower[s] P+ psi(s-1),  s +- 1 mod Ls,
+ * P+ keeping spins 0,1 and P- spins 2,3; dag = 1 applies the exact adjoint of the same A (Grid's
+ * M5Ddag instead takes pre-shifted arrays).  Any lattice (full or half), single rhs, F64/F32/F16
+ * fields, 1 <= Ls <= 64, out != in.
+ * The Mobius operator (b, c, M5, mf): M = Mooee - 1/2 Dhop A(b, c) with
+ *   Mooee = A(diag 1 + b (4 - M5), off-diagonal -(1 - c (4 - M5))),
+ * A(d, e): diag d, lower = upper = e, the walls (upper[Ls-1], lower[0]) e -> -mf e.
+ * b = 1, c = 0 is the Shamir operator of gbdw_dwf_m. */
+int gbdw_m5d(gbdw_field* out, const gbdw_field* in, const double* lower, const double* diag,
+             const double* upper, int dag);
+/* out = A^-1 in (A^-dag for dag): two cyclic bidiagonal solves per chirality;
+ * GBDW_ERR_INVALID when A is singular */
+int gbdw_m5d_inv(gbdw_field* out, const gbdw_field* in, const double* lower, const double* diag,
+                 const double* upper, int dag);
+int gbdw_mobius_mooee(gbdw_field* out, const gbdw_field* in, double b, double c, double M5, double mf,
+                      int dag);
+int gbdw_mobius_mooee_inv(gbdw_field* out, const gbdw_field* in, double b, double c, double M5,
+                          double mf, int dag);
+/* out = M in (M^dag in for dag) on a full lattice; tmp: a field like in (distinct from out and in);
+ * |out|^2 into norm2 when non-null */
+int gbdw_mobius_m(const gbdw_gauge* g, gbdw_field* out, gbdw_field* tmp, const gbdw_field* in, double b,
+                  double c, double M5, double mf, int dag, double* norm2);
+/* even-odd hopping block on half p = g's lattice, in on half q:
+ * dag 0: out = -1/2 Dhop_pq A(b, c) in, tmp on half q;  dag 1: out = -1/2 A(b, c)^dag DhopDag_pq in,
+ * tmp on half p */
+int gbdw_mobius_meooe(const gbdw_gauge* g, gbdw_field* out, gbdw_field* tmp, const gbdw_field* in, double b,
+                      double c, double mf, int dag);
+/* Schur operator on half p: Mpc = Mooee - Meooe_pq Mooee^-1 Meooe_qp (its adjoint for dag);
+ * tp on half p, tq1 / tq2 on half q; |out|^2 into norm2 when non-null */
+int gbdw_mobius_mpc(const gbdw_gauge* gp, const gbdw_gauge* gq, gbdw_field* out, gbdw_field* tp,
+                    gbdw_field* tq1, gbdw_field* tq2, const gbdw_field* in, double b, double c, double M5,
+                    double mf, int dag, double* norm2);
+
 /* ------------------------------------------------------------------ static-data files
  * The reference's exchange format for Grid-generated test data (TableGenerate.cc:93-138,
  * read by bench.cc:55-88 and bench_simple.cc:72-84 as compiled-in arrays): static_data.h holds
