@@ -301,6 +301,28 @@ def secondary(gb, args, peak) -> dict:
         "hbm_frac": round(algo_bytes(1, 1, LS) * V5 / 2 / t / 1e9 / peak, 3), "launch": list(gb.tune_query(g32, x32)),
         "m5inv_ms": round(t5 * 1e3, 4), "m5inv_hbm_frac": round(2 * 96 * V5 / 2 / t5 / 1e9 / peak, 3)}
     del ge, xo, ye, ze, le, lo
+    # Mobius (b = 1.5, c = 0.5): M = Mooee - 1/2 Dhop A(b, c) is one 5th-dimension pass and the
+    # hopping pass with the Mooee epilogue; the 5th-dimension pass alone is HBM bound (one FP32
+    # spinor read and one written per 5D site)
+    t32 = gb.Field(lat, gb.F32)
+
+    def per_call(fn):
+        for _ in range(5):
+            fn()
+        gb.synchronize()
+        tm.start()
+        for _ in range(steps):
+            fn()
+        return tm.stop() / steps / 1e3
+
+    tmob = per_call(lambda: gb.mobius_m(g32, y32, t32, x32, 1.5, 0.5, 1.8, 0.01))
+    tsham = per_call(lambda: gb.dwf_m(g32, y32, x32, 1.8, 0.01))
+    tm5d = per_call(lambda: gb.mobius_mooee(t32, x32, 1.5, 0.5, 1.8, 0.01))
+    out["mobius_m_f32_16^4x16"] = {
+        "ms": round(tmob * 1e3, 4), "shamir_m_ms": round(tsham * 1e3, 4),
+        "m5d_ms": round(tm5d * 1e3, 4), "m5d_hbm_frac": round(2 * 96 * V5 / tm5d / 1e9 / peak, 3),
+        "b": 1.5, "c": 0.5, "M5": 1.8, "mf": 0.01}
+    del t32
     del g64, g32, g16, x64, y64, x32, y32, x16, y16, lat
     if not args.quick:
         out["multi_rhs_24^4x12_k12"] = bench_mrhs(gb, peak)

@@ -20,7 +20,7 @@ __all__ = ["F64", "F32", "F16", "BF16", "CG_PLAIN", "CG_MIXED", "CG_DOUBLE", "Gb
            "device_available", "launch_count", "synchronize", "seed_from_ints", "generate_gauge",
            "generate_fermion", "generate_table", "Lattice", "Gauge", "Field", "dhop", "dwf_m", "dwf_mdagm",
            "cg_solve", "Batch", "dslash_kernel", "Timer", "flush_l2", "m5d", "m5d_inv", "mobius_mooee",
-           "mobius_mooee_inv", "mobius_m", "mobius_meooe", "mobius_mpc"]
+           "mobius_mooee_inv", "mobius_m", "mobius_meooe", "mobius_mpc", "mobius_mdagm", "cg_solve_mobius"]
 
 _DT = {F64: np.float64, F32: np.float32}
 
@@ -369,6 +369,27 @@ def mobius_mpc(gp: Gauge, gq: Gauge, out: Field, tp: Field, tq1: Field, tq2: Fie
     check(load().gbdw_mobius_mpc(gp.h, gq.h, out.h, tp.h, tq1.h, tq2.h, inp.h, b, c, M5, mf, int(dag),
                                  C.byref(v) if want_norm else None))
     return v.value if want_norm else None
+
+
+def mobius_mdagm(g: Gauge, out: Field, t: Field, tmp: Field, inp: Field, b: float, c: float, M5: float,
+                 mf: float) -> float:
+    v = C.c_double()
+    check(load().gbdw_mobius_mdagm(g.h, out.h, t.h, tmp.h, inp.h, b, c, M5, mf, C.byref(v)))
+    return v.value
+
+
+def cg_solve_mobius(g64: Gauge, x: Field, b: Field, b5: float, c5: float, M5: float, mf: float, mode: int,
+                    tol: float = 1e-10, max_iter: int = 20000, delta: float = 0.1, g32: Gauge | None = None,
+                    gsloppy: Gauge | None = None, sloppy_prec: int = F16) -> dict:
+    """Mobius M^dag M x = b by CG with reliable updates (modes as cg_solve)."""
+    prm = CGParams(tol, max_iter, delta, sloppy_prec, gsloppy.prec if gsloppy is not None else F16)
+    st = CGStats()
+    status = load().gbdw_cg_solve_mobius(g64.h, g32.h if g32 is not None else None,
+                                         gsloppy.h if gsloppy is not None else None, x.h, b.h, b5, c5, M5, mf,
+                                         mode, C.byref(prm), C.byref(st))
+    check(status)
+    return {"iterations": st.iterations, "reliable_updates": st.reliable_updates,
+            "true_residual": st.true_residual, "seconds": st.seconds, "final_rr": st.final_rr}
 
 
 def cg_solve(g64: Gauge, x: Field, b: Field, M5: float, mf: float, mode: int, tol: float = 1e-10,

@@ -98,6 +98,9 @@ PROTOTYPES = {
     "gbdw_mobius_m": (_i, [_vp, _vp, _vp, _vp, _d, _d, _d, _d, _i, _dp]),
     "gbdw_mobius_meooe": (_i, [_vp, _vp, _vp, _vp, _d, _d, _d, _i]),
     "gbdw_mobius_mpc": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, _d, _d, _d, _i, _dp]),
+    "gbdw_mobius_mdagm": (_i, [_vp, _vp, _vp, _vp, _vp, _d, _d, _d, _d, _dp]),
+    "gbdw_cg_solve_mobius": (_i, [_vp, _vp, _vp, _vp, _vp, _d, _d, _d, _d, _i, C.POINTER(CGParams),
+                                  C.POINTER(CGStats)]),
     "gbdw_static_data_info": (_i, [C.c_char_p, C.c_char_p, C.POINTER(C.c_uint64), C.POINTER(C.c_int),
                                    C.POINTER(C.c_int), C.POINTER(C.c_uint64)]),
     "gbdw_static_data_read": (_i, [C.c_char_p, _vp, _u64, _vp, _u64, _vp, _u64, _vp, _u64, _vp, _u64]),

@@ -271,6 +271,45 @@ extern "C" int gbdw_cg_solve(const gbdw_gauge* g64, const gbdw_gauge* g32, const
   return cg_core(P, mode, x, b, prm, stats, who);
 }
 
+// Mobius M^dag M x = b on the full lattice (the operator of mobius.cu), the same modes and
+// reliable updates as gbdw_cg_solve; the adjoint pass ends in a 5th-dimension kernel, so the
+// residual update runs as its own vector pass.
+extern "C" int gbdw_cg_solve_mobius(const gbdw_gauge* g64, const gbdw_gauge* g32, const gbdw_gauge* gs,
+                                    gbdw_field* x, const gbdw_field* b, double b5, double c5, double M5, double mf,
+                                    int mode, const gbdw_cg_params* prm, gbdw_cg_stats* stats) {
+  const char* who = "gbdw_cg_solve_mobius";
+  int op_prec = GBDW_F64;
+  int st;
+  TRY(check_mode(mode, g64, g32, gs, prm, who, &op_prec));
+  if (!x || !b || x->prec != GBDW_F64 || b->prec != GBDW_F64 || x->lat != g64->lat || b->lat != g64->lat ||
+      x->nrhs != 1 || b->nrhs != 1) {
+    set_error("gbdw_cg_solve_mobius: need F64 single-rhs x and b on the gauge field's lattice");
+    return GBDW_ERR_INVALID;
+  }
+  TRY(ensure_device());
+  const gbdw_lattice* lat = g64->lat;
+  Fields F;
+  gbdw_field *t64 = nullptr, *u64 = nullptr, *ts = nullptr, *us = nullptr;
+  TRY(F.make(lat, GBDW_F64, &t64));
+  TRY(F.make(lat, GBDW_F64, &u64));
+  if (op_prec != GBDW_F64) {
+    TRY(F.make(lat, op_prec, &ts));
+    TRY(F.make(lat, op_prec, &us));
+  }
+  const gbdw_gauge* gop = mode == GBDW_CG_DOUBLE ? g64 : mode == GBDW_CG_PLAIN ? g32 : gs;
+  Problem P;
+  P.lat = lat;
+  P.op_prec = op_prec;
+  P.exact = [&](gbdw_field* out, const gbdw_field* in, double* pap) {
+    return mobius_mdagm(g64, out, t64, u64, in, b5, c5, M5, mf, pap);
+  };
+  P.sloppy = [&](gbdw_field* out, const gbdw_field* in, double* pap) {
+    if (op_prec == GBDW_F64) return mobius_mdagm(gop, out, t64, u64, in, b5, c5, M5, mf, pap);
+    return mobius_mdagm(gop, out, ts, us, in, b5, c5, M5, mf, pap);
+  };
+  return cg_core(P, mode, x, b, prm, stats, who);
+}
+
 // Solves M x = b (x, b FP64 on the full lattice) by the Schur complement on the odd half:
 //   b'_o = b_o + 1/2 Dhop_oe D5^-1 b_e,   Mpc^dag Mpc x_o = Mpc^dag b'_o (CG, reliable updates),
 //   x_e  = D5^-1 (b_e + 1/2 Dhop_eo x_o).

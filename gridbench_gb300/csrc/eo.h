@@ -21,6 +21,9 @@ int mpcdagmpc(const gbdw_gauge* gp, const gbdw_gauge* gq, gbdw_field* out, gbdw_
 int mpcdagmpc_residual(const gbdw_gauge* gp, const gbdw_gauge* gq, gbdw_field* sink, gbdw_field* tp, gbdw_field* tq1,
                        gbdw_field* tq2, gbdw_field* r, const gbdw_field* in, double M5, double mf, double rr,
                        double out[3]);
+// Mobius M^dag M on a full lattice (mobius.cu); t, tmp temporaries like in; pap = |M in|^2
+int mobius_mdagm(const gbdw_gauge* g, gbdw_field* out, gbdw_field* t, gbdw_field* tmp, const gbdw_field* in,
+                 double b, double c, double M5, double mf, double* pap);
 int field_pick(gbdw_field* half, const gbdw_field* full);
 int field_place(gbdw_field* full, const gbdw_field* half);
 }  // namespace gbdw

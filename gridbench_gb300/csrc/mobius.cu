@@ -515,6 +515,36 @@ int mobius_mpc(const gbdw_gauge* gp, const gbdw_gauge* gq, gbdw_field* out, gbdw
 
 }  // namespace
 
+int mobius_mdagm(const gbdw_gauge* g, gbdw_field* out, gbdw_field* t, gbdw_field* tmp, const gbdw_field* in,
+                 double b, double c, double M5, double mf, double* pap) {
+  const Mobius m{b, c, M5, mf};
+  if (int st = check_operands(g, t, in, true)) return st;
+  if (int st = check_operands(g, tmp, in, true)) return st;
+  if (int st = check_operands(g, out, in, true)) return st;
+  if (t == tmp || out == t || out == tmp) {
+    set_error("Mobius M^dag M: out, t and tmp must be distinct");
+    return GBDW_ERR_INVALID;
+  }
+  if (!check_mobius(m)) return GBDW_ERR_INVALID;
+  if (int st = check_ls(in)) return st;
+  const int Ls = in->lat->Ls;
+  // t = M in with |t|^2 reduced in the hopping pass and read after the adjoint passes
+  if (int st = m5d(tmp, in, meo5(Ls, m, 1.0), nullptr, nullptr, 0)) return st;
+  DhopExtra ex;
+  ex.c5 = m.cee();
+  double dummy = 0.0;
+  if (int st = run_dhop(g, t, tmp, 0, 1, m.bee(), m.mf, pap ? &dummy : nullptr, false, in, 0.5, &ex)) return st;
+  if (int st = run_dhop(g, tmp, t, 1, 0, 0.0, 0.0, nullptr)) return st;
+  const Coef5 b5 = meo5(Ls, m, -0.5);
+  if (int st = m5d(out, t, mooee(Ls, m), tmp, &b5, 1)) return st;
+  if (pap) {
+    Reduce red;
+    if (int st = reduce_scratch(1, 1, &red)) return st;
+    return reduce_fetch(red, 1, pap);
+  }
+  return GBDW_OK;
+}
+
 }  // namespace gbdw
 
 using namespace gbdw;
@@ -565,6 +595,12 @@ int gbdw_mobius_meooe(const gbdw_gauge* g, gbdw_field* out, gbdw_field* tmp, con
                       double mf, int dag) {
   if (int st = ensure_device()) return st;
   return mobius_meooe(g, out, tmp, in, Mobius{b, c, 0.0, mf}, dag ? 1 : 0);
+}
+
+int gbdw_mobius_mdagm(const gbdw_gauge* g, gbdw_field* out, gbdw_field* t, gbdw_field* tmp, const gbdw_field* in,
+                      double b, double c, double M5, double mf, double* pap) {
+  if (int st = ensure_device()) return st;
+  return mobius_mdagm(g, out, t, tmp, in, b, c, M5, mf, pap);
 }
 
 int gbdw_mobius_mpc(const gbdw_gauge* gp, const gbdw_gauge* gq, gbdw_field* out, gbdw_field* tp, gbdw_field* tq1,

@@ -265,6 +265,16 @@ int gbdw_mobius_meooe(const gbdw_gauge* g, gbdw_field* out, gbdw_field* tmp, con
 int gbdw_mobius_mpc(const gbdw_gauge* gp, const gbdw_gauge* gq, gbdw_field* out, gbdw_field* tp,
                     gbdw_field* tq1, gbdw_field* tq2, const gbdw_field* in, double b, double c, double M5,
                     double mf, int dag, double* norm2);
+/* out = M^dag M in (full lattice); t, tmp temporaries like in (out, t, tmp distinct);
+ * pap = |M in|^2 when non-null */
+int gbdw_mobius_mdagm(const gbdw_gauge* g, gbdw_field* out, gbdw_field* t, gbdw_field* tmp,
+                      const gbdw_field* in, double b, double c, double M5, double mf, double* pap);
+/* Solves M^dag M x = b for the Mobius operator (x, b F64 on the full lattice; x holds the initial
+ * guess) with the modes, gauge fields and reliable updates of gbdw_cg_solve. */
+int gbdw_cg_solve_mobius(const gbdw_gauge* g_double, const gbdw_gauge* g_single,
+                         const gbdw_gauge* g_sloppy, gbdw_field* x, const gbdw_field* b, double b5,
+                         double c5, double M5, double mf, int mode, const gbdw_cg_params* prm,
+                         gbdw_cg_stats* stats);
 
 /* ------------------------------------------------------------------ static-data files
  * The reference's exchange format for Grid-generated test data (TableGenerate.cc:93-138,

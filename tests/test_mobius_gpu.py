@@ -168,3 +168,39 @@ def test_mobius_schur_operator(gpu, prec):
         gb.mobius_mpc(go, ge, mdx, tp, tq1, tq2, xo, B5, C5, M5, MF, 1)
         a, b = xo.dot(my), mdx.dot(y)
         assert abs(a - b) / abs(a) < 1e-13
+
+
+def test_mobius_mdagm_matches_oracle(gpu):
+    Ls = 8
+    c = make_case((4, 4, 2, 4), Ls)
+    lat = gb.Lattice.from_table(c["nbr"], c["prm"], c["nsite"], Ls)
+    g = gb.Gauge(lat, c["U"], gb.F64)
+    x = gb.Field(lat, gb.F64).load(c["phi"])
+    out, t, tmp = gb.Field(lat, gb.F64), gb.Field(lat, gb.F64), gb.Field(lat, gb.F64)
+    pap = gb.mobius_mdagm(g, out, t, tmp, x, B5, C5, M5, MF)
+    m = mob.mobius_m(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], Ls, B5, C5, M5, MF, 0)
+    ref = mob.mobius_m(c["U"], m, c["nbr"], c["prm"], c["nsite"], Ls, B5, C5, M5, MF, 1)
+    assert rel_err(out.numpy(), ref) < 1e-13
+    assert abs(pap - float(np.sum(m ** 2))) / pap < 1e-12
+
+
+@pytest.mark.parametrize("mode,sp", [(gb.CG_DOUBLE, gb.F16), (gb.CG_PLAIN, gb.F16), (gb.CG_MIXED, gb.F16),
+                                     (gb.CG_MIXED, gb.F32)])
+def test_mobius_cg_reaches_1e10(gpu, mode, sp):
+    """Mobius M^dag M x = b to a 1e-10 true residual, re-checked with the numpy oracle."""
+    Ls = 8
+    c = make_case((4, 4, 4, 4), Ls)
+    lat = gb.Lattice.from_table(c["nbr"], c["prm"], c["nsite"], Ls)
+    g64, g32, g16 = (gb.Gauge(lat, c["U"], p) for p in (gb.F64, gb.F32, gb.F16))
+    b = gb.Field(lat, gb.F64).load(c["phi"])
+    x = gb.Field(lat, gb.F64)
+    st = gb.cg_solve_mobius(g64, x, b, B5, C5, M5, MF, mode, tol=1e-10, max_iter=5000, delta=0.03 if sp == gb.F16
+                            else 1e-4, g32=g32, gsloppy=g16 if sp == gb.F16 else g32, sloppy_prec=sp)
+    print(mode, sp, st)
+    assert st["true_residual"] <= 1e-10
+    xv = x.numpy()
+    m = mob.mobius_m(c["U"], xv, c["nbr"], c["prm"], c["nsite"], Ls, B5, C5, M5, MF, 0)
+    ax = mob.mobius_m(c["U"], m, c["nbr"], c["prm"], c["nsite"], Ls, B5, C5, M5, MF, 1)
+    assert np.linalg.norm(c["phi"] - ax) / np.linalg.norm(c["phi"]) <= 2e-10
+    if mode != gb.CG_DOUBLE:
+        assert st["reliable_updates"] >= 1
