@@ -323,6 +323,26 @@ def secondary(gb, args, peak) -> dict:
         "m5d_ms": round(tm5d * 1e3, 4), "m5d_hbm_frac": round(2 * 96 * V5 / tm5d / 1e9 / peak, 3),
         "b": 1.5, "c": 0.5, "M5": 1.8, "mf": 0.01}
     del t32
+    # halo packing for a domain decomposition: the 8 faces' projected half spinors into device
+    # buffers (allocated through torch, plumbing only); HBM bytes = every face spinor read once,
+    # half of it written
+    try:
+        import torch
+        bufs = [torch.empty(x32.halo_bytes(mu), dtype=torch.uint8, device="cuda") for mu in range(4) for _ in (0, 1)]
+        ptrs = [gb.C.c_void_p(b.data_ptr()) for b in bufs]
+
+        def pack_all():
+            for k in range(8):
+                gb.check(gb.load().gbdw_halo_pack(x32.h, k // 2, k % 2, 0, ptrs[k]))
+
+        thalo = per_call(pack_all)
+        face5 = sum(int(np.prod(DIMS)) // DIMS[mu] for mu in range(4)) * 2 * LS
+        out["halo_pack_f32_16^4x16_8faces"] = {
+            "us": round(thalo * 1e6, 2), "face_sites5": face5, "bytes": face5 * (96 + 48),
+            "hbm_frac": round(face5 * (96 + 48) / thalo / 1e9 / peak, 3), "launches": 8}
+        del bufs
+    except ImportError:
+        pass
     del g64, g32, g16, x64, y64, x32, y32, x16, y16, lat
     if not args.quick:
         out["multi_rhs_24^4x12_k12"] = bench_mrhs(gb, peak)

@@ -224,6 +224,19 @@ class Field(_Handle):
         check(load().gbdw_field_pick(self.h, full.h))
         return self
 
+    def halo_bytes(self, mu: int) -> int:
+        n = C.c_size_t()
+        check(load().gbdw_halo_bytes(self.h, int(mu), C.byref(n)))
+        return n.value
+
+    def halo_pack(self, mu: int, face: int, dag: int = 0, out: np.ndarray | None = None) -> np.ndarray:
+        """The spin-projected half spinors of face 0 (x_mu = 0) or 1 (x_mu = L_mu - 1) that the
+        neighbouring domain reads (the transport format of include/gbdw.h), as raw bytes."""
+        if out is None:
+            out = np.empty(self.halo_bytes(mu), dtype=np.uint8)
+        check(load().gbdw_halo_pack(self.h, int(mu), int(face), int(dag), _ptr(out)))
+        return out
+
     def place_into(self, full: "Field") -> "Field":
         """full <- self on self's parity (the other parity of full is kept)"""
         check(load().gbdw_field_place(full.h, self.h))

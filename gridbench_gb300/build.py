@@ -24,7 +24,7 @@ INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_UNITS = ["context.cu", "fields.cu", "dhop.cu", "dhop_f32.cu", "dhop_f64.cu", "dhop_f16.cu",
               "blas.cu", "cg.cu", "batch.cu", "tune.cu", "dslash_api.cu", "gen_device.cu", "selftest.cu", "noalloc.cu",
-              "eo.cu", "mobius.cu"]
+              "eo.cu", "mobius.cu", "halo.cu"]
 HOST_UNITS = ["gen.cc", "static_data.cc"]
 DRIVER_SOURCES = {"bench_gb300": "bench_gb300.cc", "bench_simple_gb300": "bench_simple_gb300.cc"}
 

@@ -276,6 +276,20 @@ int gbdw_cg_solve_mobius(const gbdw_gauge* g_double, const gbdw_gauge* g_single,
                          double c5, double M5, double mf, int mode, const gbdw_cg_params* prm,
                          gbdw_cg_stats* stats);
 
+/* ------------------------------------------------------------------ halo packing
+ * No counterpart in GridBench (one node, no halo exchange): the spin-projected half spinors a
+ * neighbouring domain of a 4D decomposition reads across one face of this field's local volume,
+ * as Grid's Wilson compressor sends them.  face 0 (x_mu = 0) feeds the domain at -mu through
+ * its forward leg mu, face 1 (x_mu = L_mu - 1) the domain at +mu through its backward leg mu+4;
+ * dag = 1 packs for DhopDag.  Layout: face site (other coordinates lexicographic, lowest
+ * dimension fastest) x 6 rows (h0 colours 0..2, h1 colours 0..2) x the field's slices in its
+ * storage format (F64 double2 per slice; F32/F16 slice pairs (Re s, Re s+1, Im s, Im s+1) over the
+ * field's padded slot count); F16 appends one FP32 norm per (face site, slice).  Fields on a
+ * periodic lattice from gbdw_lattice_create; dst is device memory (16-byte aligned) or host
+ * memory (copied back before returning). */
+int gbdw_halo_bytes(const gbdw_field* f, int mu, size_t* bytes);
+int gbdw_halo_pack(const gbdw_field* f, int mu, int face, int dag, void* dst);
+
 /* ------------------------------------------------------------------ static-data files
  * The reference's exchange format for Grid-generated test data (TableGenerate.cc:93-138,
  * read by bench.cc:55-88 and bench_simple.cc:72-84 as compiled-in arrays): static_data.h holds
