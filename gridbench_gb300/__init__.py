@@ -237,6 +237,12 @@ class Field(_Handle):
         check(load().gbdw_halo_pack(self.h, int(mu), int(face), int(dag), _ptr(out)))
         return out
 
+    def halo_pack_all(self, dst_ptrs, dag: int = 0) -> None:
+        """All eight faces in one launch into device buffers; dst_ptrs[2*mu + face] are device
+        addresses (16-byte aligned) of halo_bytes(mu) bytes each."""
+        arr = (C.c_void_p * 8)(*[int(q) for q in dst_ptrs])
+        check(load().gbdw_halo_pack_all(self.h, int(dag), arr))
+
     def place_into(self, full: "Field") -> "Field":
         """full <- self on self's parity (the other parity of full is kept)"""
         check(load().gbdw_field_place(full.h, self.h))

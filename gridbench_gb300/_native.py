@@ -101,6 +101,7 @@ PROTOTYPES = {
     "gbdw_mobius_mdagm": (_i, [_vp, _vp, _vp, _vp, _vp, _d, _d, _d, _d, _dp]),
     "gbdw_halo_bytes": (_i, [_vp, _i, C.POINTER(C.c_size_t)]),
     "gbdw_halo_pack": (_i, [_vp, _i, _i, _i, _vp]),
+    "gbdw_halo_pack_all": (_i, [_vp, _i, C.POINTER(C.c_void_p)]),
     "gbdw_cg_solve_mobius": (_i, [_vp, _vp, _vp, _vp, _vp, _d, _d, _d, _d, _i, C.POINTER(CGParams),
                                   C.POINTER(CGStats)]),
     "gbdw_static_data_info": (_i, [C.c_char_p, C.c_char_p, C.POINTER(C.c_uint64), C.POINTER(C.c_int),

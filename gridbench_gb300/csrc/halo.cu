@@ -17,8 +17,9 @@
 // slices in its own storage format (F64: double2 per slice; F32/F16: slice pairs stored as
 // (Re s, Re s+1, Im s, Im s+1) over LsP slots); for F16 a block of nface * LsE FP32 norms (the
 // largest |component| of each slice's packed half spinor) follows the values.
-// One thread per (face site, slice): every face spinor is read once, 6 of its 12 complex
-// components are written -- HBM bound, 1.5 spinors of traffic per packed 5D site.
+// One thread per (face site, slice pair) over all requested faces in one launch: every face
+// spinor is read once, 6 of its 12 complex components are written -- HBM bound, 1.5 spinors of
+// traffic per packed 5D site.
 #include <algorithm>
 #include <cmath>
 
@@ -40,33 +41,38 @@ __device__ __forceinline__ cpx<T> unit_times(cpx<T> a) {
   else return {a.i, -a.r};                          // -i a
 }
 
+// One launch packs up to 8 faces: thread -> (face k, face site f, first slice e0 of N).
+struct HaloFace {
+  void* out;
+  float* out_norm;
+  int64_t nface;
+  int64_t first;  // first thread of this face
+  int mu;
+  int xmu;  // the face's coordinate in direction mu
+  int leg;  // the receiving leg whose projector applies (after dag)
+};
+
 struct HaloParams {
   const void* in;
   const float* in_norm;
-  void* out;
-  float* out_norm;
   int dims[4];
-  int mu;
-  int xmu;  // the face's coordinate in direction mu
-  int64_t nface;
   int LsE;
   int LsP;
+  int nfaces;
+  int64_t total;  // threads over all faces
+  HaloFace face[8];
 };
 
-template <int P, int LT>
-__global__ void __launch_bounds__(256) k_halo_pack(const HaloParams p) {
+template <int P, int LT, int N>
+__device__ __forceinline__ void pack_face(const HaloParams& p, const HaloFace& F, int64_t f, int e0) {
   using T = typename Arith<P>::T;
   using S = LegSpin<LT>;
-  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (i >= p.nface * p.LsE) return;
-  const int64_t f = i / p.LsE;
-  const int e = int(i - f * p.LsE);
   int c[4];
   int64_t r = f;
 #pragma unroll
   for (int d = 0; d < 4; ++d) {
-    if (d == p.mu) {
-      c[d] = p.xmu;
+    if (d == F.mu) {
+      c[d] = F.xmu;
     } else {
       c[d] = int(r % p.dims[d]);
       r /= p.dims[d];
@@ -74,34 +80,76 @@ __global__ void __launch_bounds__(256) k_halo_pack(const HaloParams p) {
   }
   const int64_t site = c[0] + int64_t(p.dims[0]) * (c[1] + int64_t(p.dims[1]) * (c[2] + int64_t(p.dims[2]) * c[3]));
   const int64_t row0 = site * 12;
-  cpx<T> h[6];
+  cpx<T> h[6][N];
 #pragma unroll
   for (int col = 0; col < 3; ++col) {
-    const cpx<T> x = Elem<P>::ld(p.in, row0 + 0 * 3 + col, e, p.LsP);
-    const cpx<T> y = Elem<P>::ld(p.in, row0 + S::A * 3 + col, e, p.LsP);
-    const cpx<T> z = Elem<P>::ld(p.in, row0 + 1 * 3 + col, e, p.LsP);
-    const cpx<T> w = Elem<P>::ld(p.in, row0 + S::B * 3 + col, e, p.LsP);
-    const cpx<T> ya = unit_times<T, S::C0>(y), wb = unit_times<T, S::C1>(w);
-    h[col] = {x.r + ya.r, x.i + ya.i};
-    h[3 + col] = {z.r + wb.r, z.i + wb.i};
+    cpx<T> x[N], y[N], z[N], w[N];
+    Vec<P, N>::load(p.in, row0 + 0 * 3 + col, e0, p.LsP, x);
+    Vec<P, N>::load(p.in, row0 + S::A * 3 + col, e0, p.LsP, y);
+    Vec<P, N>::load(p.in, row0 + 1 * 3 + col, e0, p.LsP, z);
+    Vec<P, N>::load(p.in, row0 + S::B * 3 + col, e0, p.LsP, w);
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      const cpx<T> ya = unit_times<T, S::C0>(y[j]), wb = unit_times<T, S::C1>(w[j]);
+      h[col][j] = {x[j].r + ya.r, x[j].i + ya.i};
+      h[3 + col][j] = {z[j].r + wb.r, z[j].i + wb.i};
+    }
   }
   const int64_t orow = f * 6;
   if constexpr (P == GBDW_F16) {
-    // dequantise with the source slice's norm, renormalise the half spinor
-    const float n = __ldg(p.in_norm + site * p.LsE + e);
-    float m = 0.f;
+    // dequantise with the source slices' norms, renormalise each slice's half spinor
+    float n[N], m[N], sc[N];
+    load_norms<N>(p.in_norm, site * p.LsE + e0, n);
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      m[j] = 0.f;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        h[k][j] = {h[k][j].r * n[j], h[k][j].i * n[j]};
+        m[j] = fmaxf(m[j], fmaxf(fabsf(h[k][j].r), fabsf(h[k][j].i)));
+      }
+      sc[j] = m[j] > 0.f ? 1.0f / m[j] : 0.f;
+    }
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
-      h[k] = {h[k].r * n, h[k].i * n};
-      m = fmaxf(m, fmaxf(fabsf(h[k].r), fabsf(h[k].i)));
-    }
-    const float s = m > 0.f ? 1.0f / m : 0.f;
+      cpx<float> v[N];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) Elem<P>::st(p.out, orow + k, e, p.LsP, h[k].r * s, h[k].i * s);
-    p.out_norm[f * p.LsE + e] = m;
+      for (int j = 0; j < N; ++j) v[j] = {h[k][j].r * sc[j], h[k][j].i * sc[j]};
+      Vec<P, N>::store_scaled(F.out, orow + k, e0, p.LsP, v);
+    }
+#pragma unroll
+    for (int j = 0; j < N; ++j) F.out_norm[f * p.LsE + e0 + j] = m[j];
   } else {
 #pragma unroll
-    for (int k = 0; k < 6; ++k) Elem<P>::st(p.out, orow + k, e, p.LsP, h[k].r, h[k].i);
+    for (int k = 0; k < 6; ++k) {
+      cpx<T> v[N];
+#pragma unroll
+      for (int j = 0; j < N; ++j) v[j] = h[k][j];
+      Vec<P, N>::store(F.out, orow + k, e0, p.LsP, v);
+    }
+  }
+}
+
+template <int P, int N>
+__global__ void __launch_bounds__(256) k_halo_pack(const __grid_constant__ HaloParams p) {
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= p.total) return;
+  int k = 0;
+  while (k + 1 < p.nfaces && i >= p.face[k + 1].first) ++k;
+  const HaloFace& F = p.face[k];
+  const int G = p.LsE / N;
+  const int64_t t = i - F.first;
+  const int64_t f = t / G;
+  const int e0 = int(t - f * G) * N;
+  switch (F.leg) {
+    case 0: pack_face<P, 0, N>(p, F, f, e0); break;
+    case 1: pack_face<P, 1, N>(p, F, f, e0); break;
+    case 2: pack_face<P, 2, N>(p, F, f, e0); break;
+    case 3: pack_face<P, 3, N>(p, F, f, e0); break;
+    case 4: pack_face<P, 4, N>(p, F, f, e0); break;
+    case 5: pack_face<P, 5, N>(p, F, f, e0); break;
+    case 6: pack_face<P, 6, N>(p, F, f, e0); break;
+    default: pack_face<P, 7, N>(p, F, f, e0); break;
   }
 }
 
@@ -136,18 +184,41 @@ int check_halo(const gbdw_field* f, int mu) {
 }
 
 template <int P>
-void launch_pack(const HaloParams& p, int leg) {
-  const unsigned g = unsigned((p.nface * p.LsE + 255) / 256);
-  switch (leg) {
-    case 0: k_halo_pack<P, 0><<<g, 256, 0, stream()>>>(p); break;
-    case 1: k_halo_pack<P, 1><<<g, 256, 0, stream()>>>(p); break;
-    case 2: k_halo_pack<P, 2><<<g, 256, 0, stream()>>>(p); break;
-    case 3: k_halo_pack<P, 3><<<g, 256, 0, stream()>>>(p); break;
-    case 4: k_halo_pack<P, 4><<<g, 256, 0, stream()>>>(p); break;
-    case 5: k_halo_pack<P, 5><<<g, 256, 0, stream()>>>(p); break;
-    case 6: k_halo_pack<P, 6><<<g, 256, 0, stream()>>>(p); break;
-    default: k_halo_pack<P, 7><<<g, 256, 0, stream()>>>(p); break;
+void launch_pack(const HaloParams& p, int N) {
+  const unsigned g = unsigned((p.total + 255) / 256);
+  if (N == 2) k_halo_pack<P, 2><<<g, 256, 0, stream()>>>(p);
+  else k_halo_pack<P, 1><<<g, 256, 0, stream()>>>(p);
+}
+
+// Packs the faces (mu[k], face[k]) into device buffers dst[k] in one launch.
+int pack_faces(const gbdw_field* f, int n, const int* mu, const int* face, int dag, void* const* dst) {
+  HaloParams p;
+  p.in = f->d;
+  p.in_norm = f->norm;
+  for (int k = 0; k < 4; ++k) p.dims[k] = f->lat->dims[k];
+  p.LsE = f->LsE;
+  p.LsP = f->LsP;
+  p.nfaces = n;
+  const int N = (f->prec != GBDW_F64 && f->LsE % 2 == 0) ? 2 : 1;
+  int64_t first = 0;
+  for (int k = 0; k < n; ++k) {
+    HaloFace& F = p.face[k];
+    F.out = dst[k];
+    F.out_norm = f->prec == GBDW_F16 ? (float*)((char*)dst[k] + halo_value_bytes(f, mu[k])) : nullptr;
+    F.nface = face_sites(f->lat, mu[k]);
+    F.first = first;
+    F.mu = mu[k];
+    F.xmu = face[k] == 0 ? 0 : f->lat->dims[mu[k]] - 1;
+    // the receiving leg: forward mu for the low face, backward mu + 4 for the high face
+    F.leg = (face[k] == 0 ? mu[k] : mu[k] + 4) ^ (dag ? 4 : 0);
+    first += F.nface * (f->LsE / N);
   }
+  p.total = first;
+  if (f->prec == GBDW_F64) launch_pack<GBDW_F64>(p, N);
+  else if (f->prec == GBDW_F32) launch_pack<GBDW_F32>(p, N);
+  else launch_pack<GBDW_F16>(p, N);
+  GBDW_LAUNCHED();
+  return GBDW_OK;
 }
 
 }  // namespace
@@ -188,28 +259,28 @@ int gbdw_halo_pack(const gbdw_field* f, int mu, int face, int dag, void* dst) {
     set_error("gbdw_halo_pack: a device destination must be 16-byte aligned");
     return GBDW_ERR_INVALID;
   }
-  HaloParams p;
-  p.in = f->d;
-  p.in_norm = f->norm;
-  p.out = d;
-  p.out_norm = f->prec == GBDW_F16 ? (float*)((char*)d + halo_value_bytes(f, mu)) : nullptr;
-  for (int k = 0; k < 4; ++k) p.dims[k] = f->lat->dims[k];
-  p.mu = mu;
-  p.xmu = face == 0 ? 0 : f->lat->dims[mu] - 1;
-  p.nface = face_sites(f->lat, mu);
-  p.LsE = f->LsE;
-  p.LsP = f->LsP;
-  // the receiving leg: forward mu for the low face, backward mu + 4 for the high face
-  const int leg = (face == 0 ? mu : mu + 4) ^ (dag ? 4 : 0);
-  if (f->prec == GBDW_F64) launch_pack<GBDW_F64>(p, leg);
-  else if (f->prec == GBDW_F32) launch_pack<GBDW_F32>(p, leg);
-  else launch_pack<GBDW_F16>(p, leg);
-  GBDW_LAUNCHED();
+  if (int st = pack_faces(f, 1, &mu, &face, dag, &d)) return st;
   if (!dev) {
     GBDW_CUDA(cudaMemcpyAsync(dst, d, bytes, cudaMemcpyDeviceToHost, stream()));
     GBDW_CUDA(cudaStreamSynchronize(stream()));
   }
   return GBDW_OK;
+}
+
+int gbdw_halo_pack_all(const gbdw_field* f, int dag, void* const dst[8]) {
+  if (int st = check_halo(f, 0)) return st;
+  if (!dst) {
+    set_error("gbdw_halo_pack_all: eight destinations");
+    return GBDW_ERR_INVALID;
+  }
+  if (int st = ensure_device()) return st;
+  for (int k = 0; k < 8; ++k)
+    if (!dst[k] || !is_device_ptr(dst[k]) || (uintptr_t(dst[k]) & 15) != 0) {
+      set_error("gbdw_halo_pack_all: eight 16-byte aligned device destinations");
+      return GBDW_ERR_INVALID;
+    }
+  const int mu[8] = {0, 0, 1, 1, 2, 2, 3, 3}, face[8] = {0, 1, 0, 1, 0, 1, 0, 1};
+  return pack_faces(f, 8, mu, face, dag, dst);
 }
 
 }  // extern "C"

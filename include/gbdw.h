@@ -289,6 +289,9 @@ int gbdw_cg_solve_mobius(const gbdw_gauge* g_double, const gbdw_gauge* g_single,
  * memory (copied back before returning). */
 int gbdw_halo_bytes(const gbdw_field* f, int mu, size_t* bytes);
 int gbdw_halo_pack(const gbdw_field* f, int mu, int face, int dag, void* dst);
+/* all eight faces in one launch: dst[2*mu + face], each a 16-byte aligned device buffer of
+ * gbdw_halo_bytes(f, mu) bytes */
+int gbdw_halo_pack_all(const gbdw_field* f, int dag, void* const dst[8]);
 
 /* ------------------------------------------------------------------ static-data files
  * The reference's exchange format for Grid-generated test data (TableGenerate.cc:93-138,

@@ -93,3 +93,29 @@ def test_pack_into_device_memory(gpu):
     gb.check(gb.load().gbdw_halo_pack(f.h, 1, 1, 0, gb.C.c_void_p(dev.data_ptr())))
     gb.synchronize()
     assert np.array_equal(dev.cpu().numpy(), host)
+
+
+@pytest.mark.parametrize("prec", [gb.F64, gb.F32, gb.F16])
+@pytest.mark.parametrize("Ls", [5, 8])
+def test_pack_all_faces_one_launch(gpu, prec, Ls):
+    """The eight faces of one launch equal the single-face packs byte for byte."""
+    torch = pytest.importorskip("torch")
+    dims = (4, 2, 6, 4)
+    c = make_case(dims, Ls)
+    f = gb.Field(gb.Lattice.periodic(dims, Ls), prec).load(c["phi"])
+    for dag in (0, 1):
+        bufs = [torch.zeros(f.halo_bytes(k // 2), dtype=torch.uint8, device="cuda") for k in range(8)]
+        n0 = gb.launch_count()
+        f.halo_pack_all([b.data_ptr() for b in bufs], dag)
+        assert gb.launch_count() - n0 == 1
+        gb.synchronize()
+        for k in range(8):
+            one = f.halo_pack(k // 2, k % 2, dag)
+            got = bufs[k].cpu().numpy()
+            LsP = Ls if prec == gb.F64 else Ls + (Ls & 1)
+            if LsP == Ls:
+                assert np.array_equal(got, one), k
+            else:  # the padded slot of odd extents is not written
+                nface = int(np.prod(dims)) // dims[k // 2]
+                assert rel_err(parse(got, prec, nface, Ls).reshape(-1).view(np.float64),
+                               parse(one, prec, nface, Ls).reshape(-1).view(np.float64)) == 0.0
