@@ -20,7 +20,7 @@ __all__ = ["F64", "F32", "F16", "BF16", "CG_PLAIN", "CG_MIXED", "CG_DOUBLE", "Gb
            "device_available", "launch_count", "synchronize", "seed_from_ints", "generate_gauge",
            "generate_fermion", "generate_table", "Lattice", "Gauge", "Field", "dhop", "dwf_m", "dwf_mdagm",
            "cg_solve", "Batch", "dslash_kernel", "Timer", "flush_l2", "m5d", "m5d_inv", "mobius_mooee",
-           "mobius_mooee_inv", "mobius_m", "mobius_meooe", "mobius_mpc", "mobius_mdagm", "cg_solve_mobius"]
+           "mobius_mooee_inv", "mobius_m", "mobius_meooe", "mobius_mpc", "mobius_mdagm", "cg_solve_mobius", "cg_solve_mobius_eo"]
 
 _DT = {F64: np.float64, F32: np.float32}
 
@@ -407,6 +407,22 @@ def cg_solve_mobius(g64: Gauge, x: Field, b: Field, b5: float, c5: float, M5: fl
                                          gsloppy.h if gsloppy is not None else None, x.h, b.h, b5, c5, M5, mf,
                                          mode, C.byref(prm), C.byref(st))
     check(status)
+    return {"iterations": st.iterations, "reliable_updates": st.reliable_updates,
+            "true_residual": st.true_residual, "seconds": st.seconds, "final_rr": st.final_rr}
+
+
+def cg_solve_mobius_eo(g64: Sequence[Gauge], x: Field, b: Field, b5: float, c5: float, M5: float, mf: float,
+                       mode: int, tol: float = 1e-10, max_iter: int = 20000, delta: float = 0.1,
+                       g32: Sequence[Gauge] | None = None, gsloppy: Sequence[Gauge] | None = None,
+                       sloppy_prec: int = F16) -> dict:
+    """Mobius M x = b by CG on the odd Schur normal system; g64/g32/gsloppy are (even, odd)
+    gauge halves.  true_residual is the full system's |b - M x| / |b|."""
+    def pair(gs):
+        return (C.c_void_p * 2)(gs[0].h.value, gs[1].h.value) if gs is not None else None
+    prm = CGParams(tol, max_iter, delta, sloppy_prec, gsloppy[0].prec if gsloppy is not None else F16)
+    st = CGStats()
+    check(load().gbdw_cg_solve_mobius_eo(pair(g64), pair(g32), pair(gsloppy), x.h, b.h, b5, c5, M5, mf, mode,
+                                         C.byref(prm), C.byref(st)))
     return {"iterations": st.iterations, "reliable_updates": st.reliable_updates,
             "true_residual": st.true_residual, "seconds": st.seconds, "final_rr": st.final_rr}
 

@@ -99,6 +99,8 @@ PROTOTYPES = {
     "gbdw_mobius_meooe": (_i, [_vp, _vp, _vp, _vp, _d, _d, _d, _i]),
     "gbdw_mobius_mpc": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, _d, _d, _d, _i, _dp]),
     "gbdw_mobius_mdagm": (_i, [_vp, _vp, _vp, _vp, _vp, _d, _d, _d, _d, _dp]),
+    "gbdw_cg_solve_mobius_eo": (_i, [_pp, _pp, _pp, _vp, _vp, _d, _d, _d, _d, _i, C.POINTER(CGParams),
+                                     C.POINTER(CGStats)]),
     "gbdw_halo_bytes": (_i, [_vp, _i, C.POINTER(C.c_size_t)]),
     "gbdw_halo_pack": (_i, [_vp, _i, _i, _i, _vp]),
     "gbdw_halo_pack_all": (_i, [_vp, _i, C.POINTER(C.c_void_p)]),

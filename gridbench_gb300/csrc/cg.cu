@@ -310,6 +310,108 @@ extern "C" int gbdw_cg_solve_mobius(const gbdw_gauge* g64, const gbdw_gauge* g32
   return cg_core(P, mode, x, b, prm, stats, who);
 }
 
+// Solves the Mobius M x = b by the Schur complement on the odd half (the same scheme as
+// gbdw_cg_solve_eo with Mooee in place of D5 and Meooe = -1/2 Dhop A(b, c)):
+//   b'_o = b_o - Meooe_oe Mooee^-1 b_e,   Mpc^dag Mpc x_o = Mpc^dag b'_o,
+//   x_e  = Mooee^-1 (b_e - Meooe_eo x_o).
+extern "C" int gbdw_cg_solve_mobius_eo(const gbdw_gauge* const g64[2], const gbdw_gauge* const g32[2],
+                                       const gbdw_gauge* const gs[2], gbdw_field* x, const gbdw_field* b, double b5,
+                                       double c5, double M5, double mf, int mode, const gbdw_cg_params* prm,
+                                       gbdw_cg_stats* stats) {
+  const char* who = "gbdw_cg_solve_mobius_eo";
+  if (!g64 || !g64[0] || !g64[1]) {
+    set_error("gbdw_cg_solve_mobius_eo: need the two F64 gauge halves");
+    return GBDW_ERR_INVALID;
+  }
+  int op_prec = GBDW_F64, op1 = GBDW_F64;
+  int st;
+  const gbdw_gauge* e32 = g32 ? g32[0] : nullptr;
+  const gbdw_gauge* o32 = g32 ? g32[1] : nullptr;
+  const gbdw_gauge* es = gs ? gs[0] : nullptr;
+  const gbdw_gauge* os = gs ? gs[1] : nullptr;
+  TRY(check_mode(mode, g64[0], e32, es, prm, who, &op_prec));
+  TRY(check_mode(mode, g64[1], o32, os, prm, who, &op1));
+  const gbdw_lattice* le = g64[0]->lat;
+  const gbdw_lattice* lo = g64[1]->lat;
+  if (le->parity != 0 || lo->parity != 1 || le->partner != lo || !x || !b || x->prec != GBDW_F64 ||
+      b->prec != GBDW_F64 || x->lat != le->parent || b->lat != le->parent || x->nrhs != 1 || b->nrhs != 1) {
+    set_error("gbdw_cg_solve_mobius_eo: gauge halves [even, odd] of the lattice of x and b (F64, single rhs)");
+    return GBDW_ERR_INVALID;
+  }
+  TRY(ensure_device());
+  Fields F;
+  gbdw_field *be = nullptr, *bo = nullptr, *te = nullptr, *ue = nullptr, *xo = nullptr, *co = nullptr;
+  gbdw_field *to = nullptr, *po = nullptr, *pa = nullptr;
+  TRY(F.make(le, GBDW_F64, &be));
+  TRY(F.make(lo, GBDW_F64, &bo));
+  TRY(F.make(le, GBDW_F64, &te));
+  TRY(F.make(le, GBDW_F64, &ue));
+  TRY(F.make(lo, GBDW_F64, &xo));
+  TRY(F.make(lo, GBDW_F64, &co));
+  TRY(F.make(lo, GBDW_F64, &to));
+  TRY(F.make(lo, GBDW_F64, &po));
+  TRY(F.make(lo, GBDW_F64, &pa));
+  gbdw_field *ps = nullptr, *pas = nullptr, *q1s = nullptr, *q2s = nullptr;
+  if (op_prec != GBDW_F64) {
+    TRY(F.make(lo, op_prec, &ps));
+    TRY(F.make(lo, op_prec, &pas));
+    TRY(F.make(le, op_prec, &q1s));
+    TRY(F.make(le, op_prec, &q2s));
+  }
+  TRY(gbdw_synchronize());
+  const auto t0 = std::chrono::steady_clock::now();
+  // b'_o = b_o - Meooe_oe Mooee^-1 b_e;  c_o = Mpc^dag b'_o
+  TRY(field_pick(be, b));
+  TRY(field_pick(bo, b));
+  TRY(mobius_mooee_op(te, be, b5, c5, M5, mf, 0, true));
+  TRY(mobius_meooe_op(g64[1], to, ue, te, b5, c5, mf, 0));
+  TRY(blas_axpby(-1.0, to, 1.0, bo));
+  TRY(gbdw_mobius_mpc(g64[1], g64[0], co, to, te, ue, bo, b5, c5, M5, mf, 1, nullptr));
+  TRY(field_pick(xo, x));
+
+  const gbdw_gauge* gpo = mode == GBDW_CG_DOUBLE ? g64[1] : mode == GBDW_CG_PLAIN ? o32 : os;
+  const gbdw_gauge* gqe = mode == GBDW_CG_DOUBLE ? g64[0] : mode == GBDW_CG_PLAIN ? e32 : es;
+  Problem P;
+  P.lat = lo;
+  P.op_prec = op_prec;
+  P.exact = [&](gbdw_field* out, const gbdw_field* in, double* pap) {
+    return mobius_mpcdagmpc(g64[1], g64[0], out, pa, po, te, ue, in, b5, c5, M5, mf, pap);
+  };
+  P.sloppy = [&](gbdw_field* out, const gbdw_field* in, double* pap) {
+    if (op_prec == GBDW_F64) return mobius_mpcdagmpc(gpo, gqe, out, pa, po, te, ue, in, b5, c5, M5, mf, pap);
+    return mobius_mpcdagmpc(gpo, gqe, out, pas, ps, q1s, q2s, in, b5, c5, M5, mf, pap);
+  };
+  gbdw_cg_stats S{};
+  const int cst = cg_core(P, mode, xo, co, prm, &S, who);
+  if (cst != GBDW_OK && cst != GBDW_ERR_NOT_CONVERGED && cst != GBDW_ERR_DIVERGED) return cst;
+
+  // x_e = Mooee^-1 (b_e - Meooe_eo x_o)
+  TRY(mobius_meooe_op(g64[0], te, to, xo, b5, c5, mf, 0));
+  TRY(blas_axpby(1.0, be, -1.0, te));
+  TRY(mobius_mooee_op(ue, te, b5, c5, M5, mf, 0, true));
+  TRY(field_place(x, ue));
+  TRY(field_place(x, xo));
+  // full-system residual: (M x)_e = Mooee x_e + Meooe_eo x_o, (M x)_o = Mooee x_o + Meooe_oe x_e
+  double bb = 0.0, re2 = 0.0, ro2 = 0.0;
+  TRY(mobius_meooe_op(g64[0], te, to, xo, b5, c5, mf, 0));
+  TRY(mobius_mooee_op(be, ue, b5, c5, M5, mf, 0, false));
+  TRY(blas_axpby(1.0, be, 1.0, te));  // te = (M x)_e
+  TRY(field_pick(be, b));
+  TRY(blas_xmy_norm(be, te, ue, &re2));
+  TRY(field_pick(ue, x));  // x_e again (ue held the even residual)
+  TRY(mobius_meooe_op(g64[1], to, te, ue, b5, c5, mf, 0));
+  TRY(mobius_mooee_op(po, xo, b5, c5, M5, mf, 0, false));
+  TRY(blas_axpby(1.0, po, 1.0, to));  // to = (M x)_o
+  TRY(field_pick(bo, b));
+  TRY(blas_xmy_norm(bo, to, co, &ro2));
+  TRY(blas_norm2(b, &bb, true));
+  TRY(gbdw_synchronize());
+  S.true_residual = std::sqrt((re2 + ro2) / bb);
+  S.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (stats) *stats = S;
+  return cst;
+}
+
 // Solves M x = b (x, b FP64 on the full lattice) by the Schur complement on the odd half:
 //   b'_o = b_o + 1/2 Dhop_oe D5^-1 b_e,   Mpc^dag Mpc x_o = Mpc^dag b'_o (CG, reliable updates),
 //   x_e  = D5^-1 (b_e + 1/2 Dhop_eo x_o).

@@ -24,6 +24,15 @@ int mpcdagmpc_residual(const gbdw_gauge* gp, const gbdw_gauge* gq, gbdw_field* s
 // Mobius M^dag M on a full lattice (mobius.cu); t, tmp temporaries like in; pap = |M in|^2
 int mobius_mdagm(const gbdw_gauge* g, gbdw_field* out, gbdw_field* t, gbdw_field* tmp, const gbdw_field* in,
                  double b, double c, double M5, double mf, double* pap);
+// Mobius blocks (mobius.cu): Mooee / Mooee^-1 (inverse) on any lattice; the even-odd hopping
+// block on half p; Mpc^dag Mpc on half p (tpa, tp on p; tq1, tq2 on q; pap = |Mpc in|^2)
+int mobius_mooee_op(gbdw_field* out, const gbdw_field* in, double b, double c, double M5, double mf, int dag,
+                    bool inverse);
+int mobius_meooe_op(const gbdw_gauge* gp, gbdw_field* out, gbdw_field* tmp, const gbdw_field* in, double b, double c,
+                    double mf, int dag);
+int mobius_mpcdagmpc(const gbdw_gauge* gp, const gbdw_gauge* gq, gbdw_field* out, gbdw_field* tpa, gbdw_field* tp,
+                     gbdw_field* tq1, gbdw_field* tq2, const gbdw_field* in, double b, double c, double M5, double mf,
+                     double* pap);
 int field_pick(gbdw_field* half, const gbdw_field* full);
 int field_place(gbdw_field* full, const gbdw_field* half);
 }  // namespace gbdw

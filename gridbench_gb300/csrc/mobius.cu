@@ -473,8 +473,8 @@ int mobius_meooe(const gbdw_gauge* gp, gbdw_field* out, gbdw_field* tmp, const g
 
 // Schur operator on half p:  Mpc = Mooee - Meooe_pq Mooee^-1 Meooe_qp  (dag: its adjoint).
 // tp on half p; tq1, tq2 on half q.
-int mobius_mpc(const gbdw_gauge* gp, const gbdw_gauge* gq, gbdw_field* out, gbdw_field* tp, gbdw_field* tq1,
-               gbdw_field* tq2, const gbdw_field* in, const Mobius& m, int dag, double* norm2) {
+int mobius_mpc_impl(const gbdw_gauge* gp, const gbdw_gauge* gq, gbdw_field* out, gbdw_field* tp, gbdw_field* tq1,
+                    gbdw_field* tq2, const gbdw_field* in, const Mobius& m, int dag, double* norm2, bool fetch) {
   if (!gp || !gq || gq->lat != gp->lat->partner) {
     set_error("Mobius Schur operator: gauge halves must be partners");
     return GBDW_ERR_INVALID;
@@ -498,7 +498,7 @@ int mobius_mpc(const gbdw_gauge* gp, const gbdw_gauge* gq, gbdw_field* out, gbdw
     DhopExtra ex;
     ex.c5 = m.cee();
     // hop_eo takes M5 and uses 5 - M5 as the diagonal coefficient
-    return hop_eo(gp, out, tq1, 0, in, 5.0 - m.bee(), m.mf, 1.0, norm2, true, &ex);
+    return hop_eo(gp, out, tq1, 0, in, 5.0 - m.bee(), m.mf, 1.0, norm2, fetch, &ex);
   }
   // Mpc^dag = Mooee^dag - (-1/2 A^dag DhopDag_pq) Mooee^-dag (-1/2 A^dag DhopDag_qp):
   // tq1 = DhopDag_qp in;  tq2 = -1/2 A^dag tq1;  tq1 = Mooee^-dag tq2;  tp = DhopDag_pq tq1;
@@ -509,11 +509,44 @@ int mobius_mpc(const gbdw_gauge* gp, const gbdw_gauge* gq, gbdw_field* out, gbdw
   if (int st = hop_eo(gp, tp, tq1, 1, nullptr, 0.0, 0.0, 0.5, nullptr, true)) return st;
   const Coef5 neg = meo5(Ls, m, 0.5);
   if (int st = m5d(out, in, oo, tp, &neg, 1)) return st;
-  if (norm2) return blas_norm2(out, norm2, true);
+  if (norm2) return blas_norm2(out, norm2, fetch);
   return GBDW_OK;
 }
 
 }  // namespace
+
+int mobius_mooee_op(gbdw_field* out, const gbdw_field* in, double b, double c, double M5, double mf, int dag,
+                    bool inverse) {
+  const Mobius m{b, c, M5, mf};
+  if (!check_mobius(m)) return GBDW_ERR_INVALID;
+  if (int st = check_ls(in)) return st;
+  return inverse ? m5d_inv(out, in, mooee(in->lat->Ls, m), dag) : m5d(out, in, mooee(in->lat->Ls, m), nullptr, nullptr, dag);
+}
+
+int mobius_meooe_op(const gbdw_gauge* gp, gbdw_field* out, gbdw_field* tmp, const gbdw_field* in, double b, double c,
+                    double mf, int dag) {
+  return mobius_meooe(gp, out, tmp, in, Mobius{b, c, 0.0, mf}, dag);
+}
+
+int mobius_mpcdagmpc(const gbdw_gauge* gp, const gbdw_gauge* gq, gbdw_field* out, gbdw_field* tpa, gbdw_field* tp,
+                     gbdw_field* tq1, gbdw_field* tq2, const gbdw_field* in, double b, double c, double M5, double mf,
+                     double* pap) {
+  if (!tpa || tpa == in || tpa == out || tpa == tp) {
+    set_error("Mobius Schur normal operator: a distinct temporary for Mpc in");
+    return GBDW_ERR_INVALID;
+  }
+  const Mobius m{b, c, M5, mf};
+  // |Mpc in|^2 stays in the reduction result: nothing between the two Schur passes reduces
+  double dummy = 0.0;
+  if (int st = mobius_mpc_impl(gp, gq, tpa, tp, tq1, tq2, in, m, 0, pap ? &dummy : nullptr, false)) return st;
+  if (int st = mobius_mpc_impl(gp, gq, out, tp, tq1, tq2, tpa, m, 1, nullptr, true)) return st;
+  if (pap) {
+    Reduce red;
+    if (int st = reduce_scratch(1, 1, &red)) return st;
+    return reduce_fetch(red, 1, pap);
+  }
+  return GBDW_OK;
+}
 
 int mobius_mdagm(const gbdw_gauge* g, gbdw_field* out, gbdw_field* t, gbdw_field* tmp, const gbdw_field* in,
                  double b, double c, double M5, double mf, double* pap) {
@@ -607,7 +640,7 @@ int gbdw_mobius_mpc(const gbdw_gauge* gp, const gbdw_gauge* gq, gbdw_field* out,
                     gbdw_field* tq2, const gbdw_field* in, double b, double c, double M5, double mf, int dag,
                     double* norm2) {
   if (int st = ensure_device()) return st;
-  return mobius_mpc(gp, gq, out, tp, tq1, tq2, in, Mobius{b, c, M5, mf}, dag ? 1 : 0, norm2);
+  return mobius_mpc_impl(gp, gq, out, tp, tq1, tq2, in, Mobius{b, c, M5, mf}, dag ? 1 : 0, norm2, true);
 }
 
 }  // extern "C"

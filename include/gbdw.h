@@ -276,6 +276,14 @@ int gbdw_cg_solve_mobius(const gbdw_gauge* g_double, const gbdw_gauge* g_single,
                          double c5, double M5, double mf, int mode, const gbdw_cg_params* prm,
                          gbdw_cg_stats* stats);
 
+/* Solves the Mobius M x = b (x, b F64 on the full lattice) by CG on the odd Schur normal system
+ * Mpc^dag Mpc (Mpc = Mooee - Meooe_oe Mooee^-1 Meooe_eo), with the modes, gauge halves and
+ * reliable updates of gbdw_cg_solve_eo; stats->true_residual is the full system's |b - M x| / |b|. */
+int gbdw_cg_solve_mobius_eo(const gbdw_gauge* const g_double[2], const gbdw_gauge* const g_single[2],
+                            const gbdw_gauge* const g_sloppy[2], gbdw_field* x, const gbdw_field* b,
+                            double b5, double c5, double M5, double mf, int mode,
+                            const gbdw_cg_params* prm, gbdw_cg_stats* stats);
+
 /* ------------------------------------------------------------------ halo packing
  * No counterpart in GridBench (one node, no halo exchange): the spin-projected half spinors a
  * neighbouring domain of a 4D decomposition reads across one face of this field's local volume,
