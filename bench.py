@@ -730,6 +730,38 @@ def run_only(args) -> dict:
             "shape": list(gb.tune_query(g, xs[0])), "gpu_launches": int(launches)}
 
 
+AUX_ONLY = ("mobius_m", "halo_pack")
+
+
+def run_aux_only(args) -> dict:
+    """The Mobius operator (b = 1.5, c = 0.5, M5 = 1.8, mf = 0.01) or the one-launch pack of all
+    eight halo faces, FP32 16^4 x 16, nothing else (for profiling)."""
+    import gridbench_gb300 as gb
+    lat = gb.Lattice.periodic(DIMS, LS)
+    g = gb.Gauge(lat, None, gb.F32, seed=11)
+    xs = [gb.Field(lat, gb.F32).gaussian(21 + i) for i in range(4)]
+    y, t = gb.Field(lat, gb.F32), gb.Field(lat, gb.F32)
+    if args.only == "mobius_m":
+        gb.tune_dhop(g, y, xs[0])
+        fn = lambda k: gb.mobius_m(g, y, t, xs[k % 2], 1.5, 0.5, 1.8, 0.01)  # noqa: E731
+    else:
+        import torch
+        bufs = [torch.empty(xs[0].halo_bytes(k // 2), dtype=torch.uint8, device="cuda") for k in range(8)]
+        ptrs = [b.data_ptr() for b in bufs]
+        fn = lambda k: xs[k % 4].halo_pack_all(ptrs)  # noqa: E731
+    for k in range(args.warmup):
+        fn(k)
+    gb.synchronize()
+    tm = gb.Timer()
+    n0 = gb.launch_count()
+    tm.start()
+    for k in range(args.steps):
+        fn(k)
+    ms = tm.stop()
+    return {"workload": args.only, "lattice": list(DIMS), "Ls": LS, "steps": args.steps,
+            "us_per_call": round(ms / args.steps * 1e3, 3), "gpu_launches": int(gb.launch_count() - n0)}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -743,7 +775,7 @@ def main(argv=None):
     ap.add_argument("--ref-seconds", type=float, default=30.0)
     ap.add_argument("--cg-small", action="store_true", help="CG secondary on 16^4 x 16 instead of 32^4 x 16")
     ap.add_argument("--cg-max-iter", type=int, default=20000)
-    ap.add_argument("--only", choices=sorted(ONLY) + list(CG_ONLY),
+    ap.add_argument("--only", choices=sorted(ONLY) + list(CG_ONLY) + list(AUX_ONLY),
                     help="one hopping-term workload, or one CG solve at 16^4 x 16, only (for profiling)")
     ap.add_argument("--shape", help="with --only: threads,slices_per_thread,form,stages")
     ap.add_argument("--tune-save", help="write the headline kernel's tuned shapes to this JSON file")
@@ -753,7 +785,8 @@ def main(argv=None):
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.only:
-        print(json.dumps(run_cg_only(args) if args.only in CG_ONLY else run_only(args)), flush=True)
+        run = run_cg_only if args.only in CG_ONLY else run_aux_only if args.only in AUX_ONLY else run_only
+        print(json.dumps(run(args)), flush=True)
         return
     D = Dist()
     try:
