@@ -324,12 +324,13 @@ def dwf_mpcdagmpc(gp: Gauge, gq: Gauge, out: Field, tp: Field, tq1: Field, tq2: 
 
 def cg_solve_eo(g64: Sequence[Gauge], x: Field, b: Field, M5: float, mf: float, mode: int, tol: float = 1e-10,
                 max_iter: int = 20000, delta: float = 0.1, g32: Sequence[Gauge] | None = None,
-                gsloppy: Sequence[Gauge] | None = None, sloppy_prec: int = F16) -> dict:
+                gsloppy: Sequence[Gauge] | None = None, sloppy_prec: int = F16, sloppy_residual: int = 0) -> dict:
     """M x = b by CG on the odd Schur normal system; g64/g32/gsloppy are (even, odd) gauge
     halves.  true_residual is the full system's |b - M x| / |b|."""
     def pair(gs):
         return (C.c_void_p * 2)(gs[0].h.value, gs[1].h.value) if gs is not None else None
-    prm = CGParams(tol, max_iter, delta, sloppy_prec, gsloppy[0].prec if gsloppy is not None else F16)
+    prm = CGParams(tol, max_iter, delta, sloppy_prec, gsloppy[0].prec if gsloppy is not None else F16,
+                   int(sloppy_residual))
     st = CGStats()
     status = load().gbdw_cg_solve_eo(pair(g64), pair(g32), pair(gsloppy), x.h, b.h, M5, mf, mode, C.byref(prm),
                                      C.byref(st))
@@ -399,9 +400,10 @@ def mobius_mdagm(g: Gauge, out: Field, t: Field, tmp: Field, inp: Field, b: floa
 
 def cg_solve_mobius(g64: Gauge, x: Field, b: Field, b5: float, c5: float, M5: float, mf: float, mode: int,
                     tol: float = 1e-10, max_iter: int = 20000, delta: float = 0.1, g32: Gauge | None = None,
-                    gsloppy: Gauge | None = None, sloppy_prec: int = F16) -> dict:
+                    gsloppy: Gauge | None = None, sloppy_prec: int = F16, sloppy_residual: int = 0) -> dict:
     """Mobius M^dag M x = b by CG with reliable updates (modes as cg_solve)."""
-    prm = CGParams(tol, max_iter, delta, sloppy_prec, gsloppy.prec if gsloppy is not None else F16)
+    prm = CGParams(tol, max_iter, delta, sloppy_prec, gsloppy.prec if gsloppy is not None else F16,
+                   int(sloppy_residual))
     st = CGStats()
     status = load().gbdw_cg_solve_mobius(g64.h, g32.h if g32 is not None else None,
                                          gsloppy.h if gsloppy is not None else None, x.h, b.h, b5, c5, M5, mf,
@@ -414,12 +416,13 @@ def cg_solve_mobius(g64: Gauge, x: Field, b: Field, b5: float, c5: float, M5: fl
 def cg_solve_mobius_eo(g64: Sequence[Gauge], x: Field, b: Field, b5: float, c5: float, M5: float, mf: float,
                        mode: int, tol: float = 1e-10, max_iter: int = 20000, delta: float = 0.1,
                        g32: Sequence[Gauge] | None = None, gsloppy: Sequence[Gauge] | None = None,
-                       sloppy_prec: int = F16) -> dict:
+                       sloppy_prec: int = F16, sloppy_residual: int = 0) -> dict:
     """Mobius M x = b by CG on the odd Schur normal system; g64/g32/gsloppy are (even, odd)
     gauge halves.  true_residual is the full system's |b - M x| / |b|."""
     def pair(gs):
         return (C.c_void_p * 2)(gs[0].h.value, gs[1].h.value) if gs is not None else None
-    prm = CGParams(tol, max_iter, delta, sloppy_prec, gsloppy[0].prec if gsloppy is not None else F16)
+    prm = CGParams(tol, max_iter, delta, sloppy_prec, gsloppy[0].prec if gsloppy is not None else F16,
+                   int(sloppy_residual))
     st = CGStats()
     check(load().gbdw_cg_solve_mobius_eo(pair(g64), pair(g32), pair(gsloppy), x.h, b.h, b5, c5, M5, mf, mode,
                                          C.byref(prm), C.byref(st)))
@@ -429,8 +432,11 @@ def cg_solve_mobius_eo(g64: Sequence[Gauge], x: Field, b: Field, b5: float, c5: 
 
 def cg_solve(g64: Gauge, x: Field, b: Field, M5: float, mf: float, mode: int, tol: float = 1e-10,
              max_iter: int = 20000, delta: float = 0.1, g32: Gauge | None = None, gsloppy: Gauge | None = None,
-             sloppy_prec: int = F16) -> dict:
-    prm = CGParams(tol, max_iter, delta, sloppy_prec, gsloppy.prec if gsloppy is not None else F16)
+             sloppy_prec: int = F16, sloppy_residual: int = 0) -> dict:
+    """M^dag M x = b (Shamir) by CG with reliable updates.  sloppy_residual = 1 keeps the mixed
+    mode's iterated residual in FP16 (FP16 spinors and links only)."""
+    prm = CGParams(tol, max_iter, delta, sloppy_prec, gsloppy.prec if gsloppy is not None else F16,
+                   int(sloppy_residual))
     st = CGStats()
     status = load().gbdw_cg_solve(g64.h, g32.h if g32 is not None else None,
                                   gsloppy.h if gsloppy is not None else None, x.h, b.h, M5, mf, mode,

@@ -28,7 +28,7 @@ class GbdwError(RuntimeError):
 
 class CGParams(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("delta", C.c_double),
-                ("sloppy_prec", C.c_int), ("sloppy_gauge", C.c_int)]
+                ("sloppy_prec", C.c_int), ("sloppy_gauge", C.c_int), ("sloppy_residual", C.c_int)]
 
 
 class CGStats(C.Structure):

@@ -279,6 +279,7 @@ int blas_cg_r(double alpha, gbdw_field* r, const gbdw_field* ap, double* rr) {
     GBDW_R(GBDW_F64, GBDW_F32)  // plain: FP64 vectors, FP32 operator
     GBDW_R(GBDW_F32, GBDW_F16)  // mixed, FP16 sloppy
     GBDW_R(GBDW_F32, GBDW_F32)  // mixed, FP32 sloppy
+    GBDW_R(GBDW_F16, GBDW_F16)  // mixed, FP16 sloppy with an FP16 iterated residual
     default:
       set_error("blas_cg_r: unsupported precision combination");
       return GBDW_ERR_INVALID;
@@ -304,6 +305,7 @@ int blas_cg_xp(double alpha, double beta, gbdw_field* x, gbdw_field* p, const gb
     GBDW_XP(GBDW_F64, GBDW_F64, GBDW_F64, GBDW_F32)
     GBDW_XP(GBDW_F32, GBDW_F16, GBDW_F32, -1)
     GBDW_XP(GBDW_F32, GBDW_F32, GBDW_F32, -1)
+    GBDW_XP(GBDW_F32, GBDW_F16, GBDW_F16, -1)
     default:
       set_error("blas_cg_xp: unsupported precision combination");
       return GBDW_ERR_INVALID;
@@ -329,6 +331,7 @@ int blas_cg_p(double beta, const gbdw_field* r, gbdw_field* p, gbdw_field* q) {
     GBDW_P(GBDW_F64, GBDW_F64, GBDW_F32)
     GBDW_P(GBDW_F32, GBDW_F16, -1)
     GBDW_P(GBDW_F32, GBDW_F32, -1)
+    GBDW_P(GBDW_F16, GBDW_F16, -1)
     default:
       set_error("blas_cg_p: unsupported precision combination");
       return GBDW_ERR_INVALID;

@@ -49,6 +49,7 @@ struct Problem {
   Op sloppy;                // A on fields of precision `op_prec`
   FusedOp fused;            // when set (PLAIN and MIXED): A and the r update in one pass pair
   int op_prec;              // F64 (DOUBLE), F32 (PLAIN) or the sloppy precision (MIXED)
+  bool half_residual_ok = false;  // the operator's passes accept an FP16 iterated residual
 };
 
 #define TRY(e)                      \
@@ -79,8 +80,10 @@ int cg_core(const Problem& P, int mode, gbdw_field* x, const gbdw_field* b, cons
     TRY(F.make(lat, GBDW_F32, &pq));
     TRY(F.make(lat, GBDW_F32, &ap));
   } else {
+    // the iterated residual: FP32, or FP16 on request when the whole sloppy operator is FP16
+    const int rprec = (prm->sloppy_residual == 1 && P.op_prec == GBDW_F16 && P.half_residual_ok) ? GBDW_F16 : GBDW_F32;
     TRY(F.make(lat, GBDW_F32, &xs));
-    TRY(F.make(lat, GBDW_F32, &rs));
+    TRY(F.make(lat, rprec, &rs));
     TRY(F.make(lat, P.op_prec, &p));
     TRY(F.make(lat, P.op_prec, &ap));
   }
@@ -258,6 +261,7 @@ extern "C" int gbdw_cg_solve(const gbdw_gauge* g64, const gbdw_gauge* g32, const
   Problem P;
   P.lat = lat;
   P.op_prec = op_prec;
+  P.half_residual_ok = gop && gop->prec == GBDW_F16;  // the fused adjoint pass has an FP16-r form
   P.exact = [&](gbdw_field* out, const gbdw_field* in, double* pap) {
     return gbdw_dwf_mdagm(g64, out, tmp64, in, M5, mf, pap);
   };
@@ -300,6 +304,7 @@ extern "C" int gbdw_cg_solve_mobius(const gbdw_gauge* g64, const gbdw_gauge* g32
   Problem P;
   P.lat = lat;
   P.op_prec = op_prec;
+  P.half_residual_ok = true;  // separate residual pass
   P.exact = [&](gbdw_field* out, const gbdw_field* in, double* pap) {
     return mobius_mdagm(g64, out, t64, u64, in, b5, c5, M5, mf, pap);
   };
@@ -374,6 +379,7 @@ extern "C" int gbdw_cg_solve_mobius_eo(const gbdw_gauge* const g64[2], const gbd
   Problem P;
   P.lat = lo;
   P.op_prec = op_prec;
+  P.half_residual_ok = true;  // separate residual pass
   P.exact = [&](gbdw_field* out, const gbdw_field* in, double* pap) {
     return mobius_mpcdagmpc(g64[1], g64[0], out, pa, po, te, ue, in, b5, c5, M5, mf, pap);
   };
@@ -474,6 +480,7 @@ extern "C" int gbdw_cg_solve_eo(const gbdw_gauge* const g64[2], const gbdw_gauge
   Problem P;
   P.lat = lo;
   P.op_prec = op_prec;
+  P.half_residual_ok = gpo && gqe && gpo->prec == GBDW_F16 && gqe->prec == GBDW_F16;
   P.exact = [&](gbdw_field* out, const gbdw_field* in, double* pap) {
     return mpcdagmpc(g64[1], g64[0], out, tp64, te, ue, in, M5, mf, pap);
   };

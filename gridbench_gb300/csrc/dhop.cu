@@ -76,16 +76,18 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
   const int tune_epi = epi;
   if (ex && ex->r) {
     // residual epilogue: the M pass's launch shape, r in place of the output
-    if (epi != 1 || !dag || ex->r->lat != out->lat || ex->r->nrhs != 1 || !ex->alpha ||
-        !(ex->r->prec == GBDW_F64 || ex->r->prec == GBDW_F32) || in->prec == GBDW_F64 ||
-        (ex->r->prec == GBDW_F64 && in->prec != GBDW_F32)) {
-      set_error("fused CG update: adjoint M pass, FP32/FP16 operator, FP32 or FP64 residual on its lattice");
+    if (epi != 1 || !dag || ex->r->lat != out->lat || ex->r->nrhs != 1 || !ex->alpha || in->prec == GBDW_F64 ||
+        (ex->r->prec == GBDW_F64 && in->prec != GBDW_F32) ||
+        (ex->r->prec == GBDW_F16 && (in->prec != GBDW_F16 || g->prec != GBDW_F16))) {
+      set_error("fused CG update: adjoint M pass, FP32/FP16 operator, FP32, FP64 (FP32 operator) or FP16 (FP16 "
+                "operator and links) residual on its lattice");
       return GBDW_ERR_INVALID;
     }
-    epi = ex->r->prec == GBDW_F64 ? 3 : 2;
+    epi = ex->r->prec == GBDW_F64 ? 3 : ex->r->prec == GBDW_F16 ? 4 : 2;
   }
   DhopParams p = make_params(g, out, in);
   if (ex && ex->r) {
+    p.r_norm = ex->r->norm;
     p.r = ex->r->d;
     p.rLsP = ex->r->LsP;
     p.alpha = ex->alpha;

@@ -423,6 +423,7 @@ struct DhopParams {
   // CG residual epilogues (EPI 2: FP32 r, EPI 3: FP64 r): r -= alpha * M(in) in place of
   // storing M(in), |r|^2 into the partials; alpha is read from device memory.
   void* r = nullptr;
+  float* r_norm = nullptr;  // EPI 4: FP16 r with per-slice norms
   int rLsP = 0;
   const double* alpha = nullptr;
 };
@@ -557,14 +558,29 @@ __device__ __forceinline__ void dwf_epilogue(const DhopParams& p, int64_t site, 
 }
 
 // ------------------------------------------------------------------ per-site finish
-// EPI 0: store Dhop(in); EPI 1: store M(in); EPI 2 / 3: r -= alpha M(in) with r FP32 / FP64
-// (the CG residual update fused into the operator's second pass; M(in) is not stored).
-// Returns |what was stored|^2 in part (FP32 outputs) or dpart (FP64 outputs and EPI 2/3).
+// EPI 0: store Dhop(in); EPI 1: store M(in); EPI 2 / 3 / 4: r -= alpha M(in) with r FP32 / FP64 /
+// FP16 (the CG residual update fused into the operator's second pass; M(in) is not stored).
+// Returns |what was stored|^2 in part (FP32 outputs) or dpart (FP64 outputs and EPI 2-4).
 template <int PIN, int POUT, int DAG, int N, int EPI, class T>
 __device__ __forceinline__ void finish_site(const DhopParams& p, int64_t site, int s0, int LsE, int LsP,
                                             cpx<T> (&v)[N][12], float& part, double& dpart) {
   if constexpr (EPI >= 1) dwf_epilogue<PIN, DAG, N>(p, site, s0, v);
-  if constexpr (EPI >= 2) {
+  if constexpr (EPI == 4) {
+    // FP16 r: dequantise with its per-slice norms, update in FP32, store with new norms
+    const float al = float(*p.alpha);
+    float nr[N];
+    load_norms<N>(p.r_norm, site * LsE + s0, nr);
+    cpx<float> rv[N][12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      cpx<float> x[N];
+      Vec<GBDW_F16, N>::load(p.r, site * 12 + k, s0, p.rLsP, x);
+#pragma unroll
+      for (int j = 0; j < N; ++j)
+        rv[j][k] = {fmaf(-al, float(v[j][k].r), x[j].r * nr[j]), fmaf(-al, float(v[j][k].i), x[j].i * nr[j])};
+    }
+    dpart = double(store_spinor<GBDW_F16, N>(p.r, p.r_norm, site, s0, LsE, p.rLsP, rv));
+  } else if constexpr (EPI >= 2) {
     constexpr int RP = EPI == 2 ? GBDW_F32 : GBDW_F64;
     using TR = typename Arith<RP>::T;
     const TR al = TR(*p.alpha);

@@ -112,12 +112,15 @@ int by_shape(const DhopParams& p, DhopLaunch L) {
 }
 
 // epi 0 Dhop, 1 M; the CG residual epilogues exist for the adjoint pass only: 2 (FP32 r, FP32
-// and FP16 spinors) and 3 (FP64 r, FP32 spinors).
+// and FP16 spinors), 3 (FP64 r, FP32 spinors) and 4 (FP16 r, FP16 spinors with FP16 links).
 template <int PIN, int POUT, int GP, int S1, int S2>
 int dispatch(const DhopParams& p, int dag, int epi, DhopLaunch L) {
   if (epi >= 2) {
     if constexpr (PIN == GBDW_F32 || PIN == GBDW_F16) {
       if (dag && epi == 2) return by_shape<PIN, POUT, GP, 1, 2, S1, S2>(p, L);
+    }
+    if constexpr (PIN == GBDW_F16 && GP == GBDW_F16) {
+      if (dag && epi == 4) return by_shape<PIN, POUT, GP, 1, 4, S1, S2>(p, L);
     }
     if constexpr (PIN == GBDW_F32) {
       if (dag && epi == 3) return by_shape<PIN, POUT, GP, 1, 3, S1, S2>(p, L);

@@ -175,6 +175,8 @@ typedef struct {
   double delta;         /* reliable-update threshold on |r|/max|r| (e.g. 0.1) */
   int sloppy_prec;      /* GBDW_F16 or GBDW_F32 for GBDW_CG_MIXED */
   int sloppy_gauge;     /* GBDW_F16, GBDW_BF16 or GBDW_F32 */
+  int sloppy_residual;  /* GBDW_CG_MIXED with FP16 spinors and FP16 links: 1 keeps the iterated
+                           residual in FP16 (per-slice norms) instead of FP32; 0 otherwise */
 } gbdw_cg_params;
 typedef struct {
   int iterations;

@@ -217,3 +217,21 @@ def test_eo_hopping_in_every_launch_form(gpu, shape):
         zz = z.numpy()
         assert abs(n2 - float(np.sum(zz * zz))) / n2 < 1e-5, (shape, dag)
     gb.synchronize()
+
+
+def test_eo_solver_fp16_residual(gpu):
+    """Even-odd mixed FP16 solve with an FP16 iterated residual (the fused Schur adjoint pass
+    with the FP16-r epilogue) reaches the target, and the full system's residual agrees with
+    the oracle's."""
+    dims, Ls = (4, 4, 4, 4), 8
+    c, lat, g64, le, lo, ge64, go64 = setup(dims, Ls, gb.F64)
+    g16 = gb.Gauge(lat, c["U"], gb.F16)
+    G16 = (g16.checkerboard(le), g16.checkerboard(lo))
+    b = gb.Field(lat, gb.F64).load(c["phi"])
+    x = gb.Field(lat, gb.F64)
+    st = gb.cg_solve_eo((ge64, go64), x, b, M5, MF, gb.CG_MIXED, tol=1e-10, max_iter=5000, delta=0.03,
+                        gsloppy=G16, sloppy_prec=gb.F16, sloppy_residual=1)
+    print(st)
+    m = oracle.dwf_m(c["U"], x.numpy(), c["nbr"], c["nsite"], Ls, M5, MF, 0)
+    res = np.linalg.norm(c["phi"] - m) / np.linalg.norm(c["phi"])
+    assert res < 1e-8 and abs(res - st["true_residual"]) <= 1e-3 * res + 1e-14
