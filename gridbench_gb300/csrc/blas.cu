@@ -6,6 +6,7 @@
 // the fixed-order grid reduction of common.cuh.
 #include "blas.h"
 #include "common.cuh"
+#include "dhop_kernel.cuh"
 #include "layout.cuh"
 
 #include <type_traits>
@@ -226,6 +227,85 @@ int64_t grid_for(const gbdw_field* f) {
 
 bool same_shape(const gbdw_field* a, const gbdw_field* b) { return a && b && a->lat == b->lat && a->nrhs == b->nrhs; }
 
+// ------------------------------------------------------------------ slice-pair forms
+// The hot CG updates on FP32/FP16 fields with an even slice count: one thread per (site, slice
+// pair), 128-bit (FP32) / 64-bit (FP16) loads and stores of the paired layout, one norm pair per
+// FP16 access; FP32 arithmetic as in the element-wise forms.
+template <int P>
+__device__ __forceinline__ void ld_pair(const void* d, const float* nrm, int64_t site, int e0, int LsE, int LsP,
+                                        cpx<float> (&v)[2][12]) {
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    cpx<float> x[2];
+    Vec<P, 2>::load(d, site * 12 + k, e0, LsP, x);
+    v[0][k] = x[0];
+    v[1][k] = x[1];
+  }
+  if constexpr (P == GBDW_F16) {
+    float n[2];
+    load_norms<2>(nrm, site * LsE + e0, n);
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int k = 0; k < 12; ++k) v[j][k] = {v[j][k].r * n[j], v[j][k].i * n[j]};
+  }
+}
+
+template <int PX, int PP, int PR>
+__global__ void k_cg_xp_pairs(double alpha, double beta, FieldOut x, FieldOut p, FieldRef r, int64_t nsite, int LsE) {
+  const int G = LsE / 2;
+  const int64_t n = nsite * G;
+  const float al = float(alpha), be = float(beta);
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t site = i / G;
+    const int e0 = int(i - site * G) * 2;
+    cpx<float> u[2][12], v[2][12];
+    ld_pair<PP>(p.d, p.n, site, e0, LsE, p.LsP, v);
+    ld_pair<PX>(x.d, x.n, site, e0, LsE, x.LsP, u);
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int k = 0; k < 12; ++k) u[j][k] = {fmaf(al, v[j][k].r, u[j][k].r), fmaf(al, v[j][k].i, u[j][k].i)};
+    store_spinor<PX, 2>(x.d, x.n, site, e0, LsE, x.LsP, u);
+    ld_pair<PR>(r.d, r.n, site, e0, LsE, r.LsP, u);
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int k = 0; k < 12; ++k) v[j][k] = {fmaf(be, v[j][k].r, u[j][k].r), fmaf(be, v[j][k].i, u[j][k].i)};
+    store_spinor<PP, 2>(p.d, p.n, site, e0, LsE, p.LsP, v);
+  }
+}
+
+template <int PR, int PA>
+__global__ void k_cg_r_pairs(double alpha, FieldOut r, FieldRef ap, int64_t nsite, int LsE, Reduce red) {
+  double acc[1] = {0.0};
+  const int G = LsE / 2;
+  const int64_t n = nsite * G;
+  const float al = float(alpha);
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t site = i / G;
+    const int e0 = int(i - site * G) * 2;
+    cpx<float> u[2][12], v[2][12];
+    ld_pair<PR>(r.d, r.n, site, e0, LsE, r.LsP, u);
+    ld_pair<PA>(ap.d, ap.n, site, e0, LsE, ap.LsP, v);
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int k = 0; k < 12; ++k) u[j][k] = {fmaf(-al, v[j][k].r, u[j][k].r), fmaf(-al, v[j][k].i, u[j][k].i)};
+    acc[0] += double(store_spinor<PR, 2>(r.d, r.n, site, e0, LsE, r.LsP, u));
+  }
+  grid_sum<1>(acc, red.partials, red.counter, red.result);
+}
+
+bool pairs_ok(const gbdw_field* f) { return f->prec != GBDW_F64 && f->LsE % 2 == 0 && f->LsP == f->LsE; }
+
+int64_t grid_pairs(const gbdw_field* f) {
+  const int64_t n = f->lat->nsite * (f->LsE / 2);
+  int64_t g = (n + kThreads - 1) / kThreads;
+  const int64_t cap = int64_t(num_sms()) * 8;
+  return g < cap ? (g > 0 ? g : 1) : cap;
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ internal entry points
@@ -264,11 +344,29 @@ int blas_xmy_norm(const gbdw_field* b, const gbdw_field* t, gbdw_field* r, doubl
 }
 
 int blas_cg_r(double alpha, gbdw_field* r, const gbdw_field* ap, double* rr) {
+  const int64_t ns = r->lat->nsite;
+  const int L = r->LsE;
+  if (pairs_ok(r) && pairs_ok(ap)) {
+    const int64_t g = grid_pairs(r);
+    Reduce red;
+    if (int st = reduce_scratch(g, 1, &red)) return st;
+    const int key = r->prec * 4 + ap->prec;
+    if (key == GBDW_F32 * 4 + GBDW_F32)
+      k_cg_r_pairs<GBDW_F32, GBDW_F32><<<unsigned(g), kThreads, 0, stream()>>>(alpha, out(r), ref(ap), ns, L, red);
+    else if (key == GBDW_F32 * 4 + GBDW_F16)
+      k_cg_r_pairs<GBDW_F32, GBDW_F16><<<unsigned(g), kThreads, 0, stream()>>>(alpha, out(r), ref(ap), ns, L, red);
+    else if (key == GBDW_F16 * 4 + GBDW_F16)
+      k_cg_r_pairs<GBDW_F16, GBDW_F16><<<unsigned(g), kThreads, 0, stream()>>>(alpha, out(r), ref(ap), ns, L, red);
+    else {
+      set_error("blas_cg_r: unsupported precision combination");
+      return GBDW_ERR_INVALID;
+    }
+    GBDW_LAUNCHED();
+    return reduce_fetch(red, 1, rr);
+  }
   const int64_t g = grid_for(r);
   Reduce red;
   if (int st = reduce_scratch(g, 1, &red)) return st;
-  const int64_t ns = r->lat->nsite;
-  const int L = r->LsE;
   const int key = r->prec * 4 + ap->prec;
 #define GBDW_R(PR, PA)                                                                                  \
   case PR * 4 + PA:                                                                                     \
@@ -290,9 +388,24 @@ int blas_cg_r(double alpha, gbdw_field* r, const gbdw_field* ap, double* rr) {
 }
 
 int blas_cg_xp(double alpha, double beta, gbdw_field* x, gbdw_field* p, const gbdw_field* r, gbdw_field* q) {
-  const int64_t g = grid_for(r);
   const int64_t ns = r->lat->nsite;
   const int L = r->LsE;
+  if (!q && pairs_ok(x) && pairs_ok(p) && pairs_ok(r) && x->prec == GBDW_F32) {
+    const unsigned g = unsigned(grid_pairs(r));
+    if (p->prec == GBDW_F16 && r->prec == GBDW_F16)
+      k_cg_xp_pairs<GBDW_F32, GBDW_F16, GBDW_F16><<<g, kThreads, 0, stream()>>>(alpha, beta, out(x), out(p), ref(r), ns, L);
+    else if (p->prec == GBDW_F16 && r->prec == GBDW_F32)
+      k_cg_xp_pairs<GBDW_F32, GBDW_F16, GBDW_F32><<<g, kThreads, 0, stream()>>>(alpha, beta, out(x), out(p), ref(r), ns, L);
+    else if (p->prec == GBDW_F32 && r->prec == GBDW_F32)
+      k_cg_xp_pairs<GBDW_F32, GBDW_F32, GBDW_F32><<<g, kThreads, 0, stream()>>>(alpha, beta, out(x), out(p), ref(r), ns, L);
+    else {
+      set_error("blas_cg_xp: unsupported precision combination");
+      return GBDW_ERR_INVALID;
+    }
+    GBDW_LAUNCHED();
+    return GBDW_OK;
+  }
+  const int64_t g = grid_for(r);
   const int qp = q ? q->prec : -1;
   FieldOut qo = q ? out(q) : FieldOut{nullptr, nullptr, 0};
   const int key = ((x->prec * 4 + p->prec) * 4 + r->prec) * 8 + (qp + 1);
