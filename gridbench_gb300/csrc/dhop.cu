@@ -40,6 +40,12 @@ int check_operands(const gbdw_gauge* g, const gbdw_field* out, const gbdw_field*
   return GBDW_OK;
 }
 
+bool form3_ok(const gbdw_field* in, int epi, int spt) {
+  if (in->prec == GBDW_F64 || spt != 2 || in->LsE != in->LsP) return false;
+  if (in->LsE == 16) return true;
+  return in->prec == GBDW_F32 && epi <= 1 && (in->LsE == 12 || in->LsE == 144);
+}
+
 bool blocked_ok(const gbdw_lattice* lat, const gbdw_field* in) {
   if (in->prec == GBDW_F64 || in->LsE != 16 || in->LsP != 16 || lat->parity >= 0 || !lat->fast) return false;
   for (int d = 0; d < 4; ++d)
@@ -119,7 +125,7 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
   if (staged && !tma_shape(in->prec, in->LsE, L, &NS, &tthreads, &smem)) L.mode = 0;
   // fall back before fixing the CTA size: the block count below must match the launch
   if (L.mode == 4 && !blocked_ok(g->lat, in)) L.mode = 3;
-  if (L.mode == 3 && (in->prec == GBDW_F64 || L.spt != 2 || in->LsE != 16 || in->LsP != 16)) L.mode = 0;
+  if (L.mode == 3 && !form3_ok(in, epi, L.spt)) L.mode = 0;
   if (L.mode == 3) L.threads = 64;
   if (L.mode == 4) L.threads = 128;
   const int64_t nthreads = p.nsite * (p.LsE / L.spt);

@@ -81,12 +81,22 @@ int by_shape(const DhopParams& p, DhopLaunch L) {
     if (L.spt == S1) return L.stages == 2 ? go_tma<PIN, POUT, GP, DAG, S1, EPI, 2>(p, L) : go_tma<PIN, POUT, GP, DAG, S1, EPI, 4>(p, L);
     if (L.spt == S2) return L.stages == 2 ? go_tma<PIN, POUT, GP, DAG, S2, EPI, 2>(p, L) : go_tma<PIN, POUT, GP, DAG, S2, EPI, 4>(p, L);
   } else if (L.mode == 3) {
-    // direct form, Ls = 16 rows at compile time, 64-thread CTAs, registers balanced for six
+    // direct form, Ls*nrhs rows at compile time, 64-thread CTAs, registers balanced for six
     // CTAs per SM (the hoisted loads of the specialised kernel otherwise take ~250 registers)
     if constexpr (PIN == GBDW_F32 || PIN == GBDW_F16) {
       if (L.spt == 2 && p.LsE == 16 && p.LsP == 16) {
         const unsigned blocks = unsigned((p.nsite * 8 + 63) / 64);
         k_dhop<PIN, POUT, GP, DAG, 2, EPI, 6, 16, 64><<<blocks, 64, 0, stream()>>>(p);
+        GBDW_LAUNCHED();
+        return GBDW_OK;
+      }
+    }
+    // FP32 Dhop / M at Ls*nrhs = 12 (one rhs at Ls = 12) and 144 (12 rhs at Ls = 12)
+    if constexpr (PIN == GBDW_F32 && EPI <= 1) {
+      if (L.spt == 2 && p.LsE == p.LsP && (p.LsE == 12 || p.LsE == 144)) {
+        const unsigned blocks = unsigned((p.nsite * (p.LsE / 2) + 63) / 64);
+        if (p.LsE == 12) k_dhop<PIN, POUT, GP, DAG, 2, EPI, 6, 12, 64><<<blocks, 64, 0, stream()>>>(p);
+        else k_dhop<PIN, POUT, GP, DAG, 2, EPI, 6, 144, 64><<<blocks, 64, 0, stream()>>>(p);
         GBDW_LAUNCHED();
         return GBDW_OK;
       }

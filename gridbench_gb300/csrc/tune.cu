@@ -76,7 +76,7 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
           if (tma_shape(in->prec, in->LsE, L, &ns, &tt, &sm)) cands.push_back(L);
         }
   }
-  if (in->prec != GBDW_F64 && in->LsE == 16 && in->LsP == 16) cands.push_back(DhopLaunch{64, 2, 3, 4});
+  if (form3_ok(in, 0, 2)) cands.push_back(DhopLaunch{64, 2, 3, 4});
   if (blocked_ok(g->lat, in)) cands.push_back(DhopLaunch{128, 2, 4, 4});
   cudaEvent_t a, b;
   GBDW_CUDA(cudaEventCreate(&a));
@@ -129,8 +129,9 @@ int gbdw_tune_set(const gbdw_gauge* g, const gbdw_field* in, int threads, int sp
     return GBDW_ERR_INVALID;
   }
   const DhopLaunch L{threads, spt, form, stages};
-  if (form == 3 && (spt != 2 || in->prec == GBDW_F64 || in->LsE != 16 || in->LsP != 16)) {
-    set_error("gbdw_tune_set: form 3 is the FP32/FP16 Ls*nrhs = 16 kernel with 2 slices per thread");
+  if (form == 3 && !form3_ok(in, 0, spt)) {
+    set_error("gbdw_tune_set: form 3 is the kernel with 2 slices per thread for Ls*nrhs = 16 (FP32/FP16) or "
+              "12 / 144 (FP32)");
     return GBDW_ERR_INVALID;
   }
   if (form == 4 && (spt != 2 || !blocked_ok(g->lat, in))) {

@@ -27,6 +27,9 @@ int mdagm_residual(const gbdw_gauge* g, gbdw_field* t, gbdw_field* r, const gbdw
                    double rr, double out[3]);
 int check_operands(const gbdw_gauge* g, const gbdw_field* out, const gbdw_field* in, bool need_single_rhs);
 DhopParams make_params(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in);
+// form 3 (specialised direct) applies: slice pairs, Ls*nrhs = 16 (FP32/FP16) or 12 / 144 (FP32
+// Dhop and M)
+bool form3_ok(const gbdw_field* in, int epi, int spt);
 // form 4 (blocked site order) applies: FP32/FP16, Ls*nrhs = 16, periodic lattice, even extents
 bool blocked_ok(const gbdw_lattice* lat, const gbdw_field* in);
 }  // namespace gbdw

@@ -298,3 +298,34 @@ def test_pinned_host_import_export_and_queued_export(gpu, prec):
     assert np.array_equal(hout.array, ref)
     with pytest.raises(gb.GbdwError):
         x_pinned.export_into(np.zeros(n), sync=False)
+
+
+@pytest.mark.parametrize("form", [0, 3])
+def test_fp32_ls12_and_12_rhs_specialised_kernels(gpu, form):
+    """FP32 at Ls = 12 with one right-hand side (Ls*nrhs = 12) and with 12 (144): the direct form
+    and form 3 with compile-time row strides give the oracle's Dhop / DhopDag for every rhs,
+    and M at Ls = 12."""
+    dims, Ls, k = (4, 2, 4, 2), 12, 12
+    c = make_case(dims, Ls)
+    lat = gb.Lattice.from_table(c["nbr"], c["prm"], c["nsite"], Ls)
+    g = gb.Gauge(lat, c["U"], gb.F32)
+    x1, y1 = gb.Field(lat, gb.F32).load(c["phi"]), gb.Field(lat, gb.F32)
+    X, Y = gb.Field(lat, gb.F32, k), gb.Field(lat, gb.F32, k)
+    srcs = [gb.generate_fermion(dims, Ls, 1, (5 + r, 6, 7, 8)) for r in range(k)]
+    for r in range(k):
+        X.load(srcs[r], r)
+    gb.tune_set(g, x1, 64, 2, form, 4)
+    gb.tune_set(g, X, 64, 2, form, 4)
+    assert tuple(gb.tune_query(g, X)) == (64, 2, form, 4)
+    for dag in (0, 1):
+        gb.dhop(g, y1, x1, dag)
+        ref = oracle.dslash(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], Ls, dag)
+        assert rel_err(y1.numpy(), ref) < TOL[gb.F32], dag
+        gb.dwf_m(g, y1, x1, 1.8, 0.01, dag)
+        refm = oracle.dwf_m(c["U"], c["phi"], c["nbr"], c["nsite"], Ls, 1.8, 0.01, dag)
+        assert rel_err(y1.numpy(), refm) < TOL[gb.F32], dag
+        gb.dhop(g, Y, X, dag)
+        for r in range(k):
+            ref = oracle.dslash(c["U"], srcs[r], c["nbr"], c["prm"], c["nsite"], Ls, dag)
+            assert rel_err(Y.numpy(r), ref) < TOL[gb.F32], (dag, r)
+    gb.synchronize()
