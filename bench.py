@@ -443,8 +443,8 @@ def bench_cg(gb, args) -> dict:
     """Time to a 1e-10 true residual, plain (FP32 operator, FP64 vectors) against mixed
     (FP16 or FP32 operator, reliable updates), on M^dag M x = b over the full lattice and on
     M x = b through the even-odd Schur complement.  Each mode runs at the reliable-update
-    threshold delta measured best for it on this problem (FP16 drifts fastest: 0.03; the FP32
-    operator holds to 1e-4).  The FP16 runs keep the iterated residual in FP16 as well
+    threshold delta measured best for it on this problem (FP16 drifts fastest: 0.03 on the full
+    lattice, 0.02 through the Schur complement; the FP32 operator holds to 1e-4).  The FP16 runs keep the iterated residual in FP16 as well
     (sloppy_residual = 1: same iterations and reliable updates, 6 % less time than an FP32 r)."""
     dims, Ls = ((32, 32, 32, 32), 16) if not args.cg_small else ((16, 16, 16, 16), 16)
     M5, mf = 1.8, 0.01
@@ -475,7 +475,7 @@ def bench_cg(gb, args) -> dict:
                                                            g32=g32, gsloppy=g32, sloppy_prec=gb.F32)),
         ("eo_plain_fp32_fp64res", 1e-4, lambda x, d: gb.cg_solve_eo(G64, x, b, M5, mf, gb.CG_PLAIN, max_iter=it,
                                                                     delta=d, g32=G32)),
-        ("eo_mixed_fp16", 0.03, lambda x, d: gb.cg_solve_eo(G64, x, b, M5, mf, gb.CG_MIXED, max_iter=it, delta=d,
+        ("eo_mixed_fp16", 0.02, lambda x, d: gb.cg_solve_eo(G64, x, b, M5, mf, gb.CG_MIXED, max_iter=it, delta=d,
                                                             g32=G32, gsloppy=G16, sloppy_prec=gb.F16,
                                                             sloppy_residual=1)),
         ("eo_mixed_fp32", 1e-4, lambda x, d: gb.cg_solve_eo(G64, x, b, M5, mf, gb.CG_MIXED, max_iter=it, delta=d,
@@ -696,7 +696,7 @@ def run_cg_only(args) -> dict:
         if args.only == "cg_eo_plain":
             st = gb.cg_solve_eo(G[0], x, b, M5, mf, gb.CG_PLAIN, delta=1e-4, g32=G[1])
         else:
-            st = gb.cg_solve_eo(G[0], x, b, M5, mf, gb.CG_MIXED, delta=0.03, g32=G[1], gsloppy=G[2],
+            st = gb.cg_solve_eo(G[0], x, b, M5, mf, gb.CG_MIXED, delta=0.02, g32=G[1], gsloppy=G[2],
                                 sloppy_prec=gb.F16, sloppy_residual=1)
     elif args.only == "cg_full_plain":
         st = gb.cg_solve(g64, x, b, M5, mf, gb.CG_PLAIN, delta=1e-4, g32=g32)
