@@ -91,3 +91,29 @@ def test_empty_and_oversize_inputs_are_rejected_without_a_device():
         L.gbdw_lattice_destroy(h)
     assert L.gbdw_dslash_kernel(1, 1, 1, nbr.ctypes.data, nbr.ctypes.data, nbr.ctypes.data, nbr.ctypes.data, 1, 0,
                                 None, 0, None) == _native.ERR_INVALID
+
+
+def test_struct_layouts_match_the_header():
+    """The ctypes mirrors of gbdw_cg_params / gbdw_cg_stats have the C structs' size and field
+    offsets (compiled from include/gbdw.h with the host compiler)."""
+    import subprocess
+    import tempfile
+    fields = {"gbdw_cg_params": _native.CGParams, "gbdw_cg_stats": _native.CGStats}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gbdw.h"', "int main(void) {"]
+    for cname, py in fields.items():
+        lines.append(f'  printf("{cname} %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'  printf("{cname}.{f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["  return 0;", "}"]
+    with tempfile.TemporaryDirectory() as d:
+        src, exe = os.path.join(d, "t.c"), os.path.join(d, "t")
+        open(src, "w").write("\n".join(lines) + "\n")
+        r = subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), src, "-o", exe],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        out = dict(line.split() for line in subprocess.run([exe], capture_output=True, text=True).stdout.split("\n")
+                   if line)
+    for cname, py in fields.items():
+        assert int(out[cname]) == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert int(out[f"{cname}.{f}"]) == getattr(py, f).offset, (cname, f)
