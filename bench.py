@@ -182,10 +182,25 @@ def cpu_baseline(dims, Ls, budget_s=10.0) -> dict:
     for _ in range(reps):
         oracle.dslash_sites(U, phi, out, nbr, 0, nsite, Ls)
     dt = time.perf_counter() - t
+    # the same port on one thread, for about a third of the budget
+    oracle.set_threads(1)
+    try:
+        t = time.perf_counter()
+        oracle.dslash_sites(U, phi, out, nbr, 0, nsite, Ls)
+        one1 = time.perf_counter() - t
+        reps1 = max(1, min(200, int(budget_s / 3 / max(one1, 1e-6))))
+        t = time.perf_counter()
+        for _ in range(reps1):
+            oracle.dslash_sites(U, phi, out, nbr, 0, nsite, Ls)
+        dt1 = time.perf_counter() - t
+    finally:
+        oracle.set_threads(oracle.threads())
     return {"value": round(FLOP_PER_SITE * nsite * Ls * reps / dt / 1e9, 3), "unit": "GFLOP/s",
             "cores": oracle.threads(), "kind": "port",
             "sample": f"{reps} full FP32 Dhop passes over {'x'.join(map(str, dims))} x Ls={Ls} "
-                      f"({dt:.1f} s, oracle port of dslash_simple.h with OpenMP)"}
+                      f"({dt:.1f} s, oracle port of dslash_simple.h with OpenMP)",
+            "single_thread": {"value": round(FLOP_PER_SITE * nsite * Ls * reps1 / dt1 / 1e9, 3), "cores": 1,
+                              "sample": f"{reps1} passes ({dt1:.1f} s)"}}
 
 
 def time_dhop(gb, g, pairs, steps, warmup, dag=0):

@@ -43,6 +43,9 @@ def lib():
             f = getattr(L, "or_dwf_m" + sfx)
             f.argtypes = [rp, rp, rp, _u64p, C.c_uint64, C.c_uint64, C.c_double, C.c_double, C.c_int]
             f.restype = None
+        L.or_set_threads.argtypes = [C.c_int]
+        L.or_set_threads.restype = None
+        L.or_max_threads.restype = C.c_int
         _lib = L
     return _lib
 
@@ -67,6 +70,11 @@ def threads() -> int:
     """OpenMP threads the oracle uses (OMP_NUM_THREADS or every host core)."""
     n = os.environ.get("OMP_NUM_THREADS")
     return int(n) if n and n.isdigit() else (os.cpu_count() or 1)
+
+
+def set_threads(n: int) -> None:
+    """Threads of the oracle's parallel loops from now on (restore with set_threads(threads()))."""
+    lib().or_set_threads(int(n))
 
 
 def dslash_lanes(U, phi, nbr, prm, nsite, Ls, nsimd, dag=0):
