@@ -119,3 +119,23 @@ def test_pack_all_faces_one_launch(gpu, prec, Ls):
                 nface = int(np.prod(dims)) // dims[k // 2]
                 assert rel_err(parse(got, prec, nface, Ls).reshape(-1).view(np.float64),
                                parse(one, prec, nface, Ls).reshape(-1).view(np.float64)) == 0.0
+
+
+@pytest.mark.parametrize("prec", [gb.F32, gb.F16])
+def test_pack_multi_rhs_field(gpu, prec):
+    """A field with several right-hand sides (slices rhs-innermost, e = s * nrhs + r) packs every
+    rhs's half spinors in its own slice positions."""
+    dims, Ls, k = (4, 2, 2, 4), 4, 3
+    lat = gb.Lattice.periodic(dims, Ls)
+    srcs = [gb.generate_fermion(dims, Ls, 1, (3 + r, 4, 5, 6)) for r in range(k)]
+    f = gb.Field(lat, prec, k)
+    for r in range(k):
+        f.load(srcs[r], r)
+    for mu in range(4):
+        nface = int(np.prod(dims)) // dims[mu]
+        for face in (0, 1):
+            got = parse(f.halo_pack(mu, face, 0), prec, nface, Ls * k).reshape(nface, Ls, k, 2, 3)
+            for r in range(k):
+                ref = halo.pack(srcs[r], dims, Ls, mu, face, 0)
+                assert rel_err(np.ascontiguousarray(got[:, :, r]).reshape(-1).view(np.float64),
+                               ref.reshape(-1).view(np.float64)) < TOL[prec], (mu, face, r)
