@@ -48,3 +48,30 @@ def test_m5d_inverse_and_adjoint(dag):
     a = _cdot(z, mob.m5d(x, Ls, lo, di, up, 0))
     b = _cdot(mob.m5d(z, Ls, lo, di, up, 1), x)
     assert abs(a - b) / abs(a) < 1e-13
+
+
+@pytest.mark.parametrize("Ls", [1, 4, 7])
+def test_mobius_split_equals_the_published_cayley_form(Ls):
+    """Mooee + Meooe equals the Mobius kernel as Brower, Neff and Orginos write it,
+    (b D_W + 1) psi_s + (c D_W - 1) chi_s with chi_s = P- psi_(s+1) + P+ psi_(s-1) (walls -mf) and
+    D_W = (4 - M5) - 1/2 Dhop, computed here from the Dhop oracle directly."""
+    b5, c5 = 1.5, 0.5
+    c = make_case((4, 2, 2, 4), Ls)
+    phi = c["phi"]
+    psi = phi.view(np.complex128).reshape(-1, Ls, 12)
+    chi = np.zeros_like(psi)
+    for s in range(Ls):
+        up, dn = (s + 1) % Ls, (s - 1) % Ls
+        fu = -MF if s == Ls - 1 else 1.0
+        fd = -MF if s == 0 else 1.0
+        chi[:, s, 6:] = fu * psi[:, up, 6:]   # P- psi(s+1)
+        chi[:, s, :6] = fd * psi[:, dn, :6]   # P+ psi(s-1)
+    chiv = chi.reshape(-1).view(np.float64)
+
+    def dw(v):
+        return (4.0 - M5) * v - 0.5 * oracle.dslash(c["U"], np.ascontiguousarray(v), c["nbr"], c["prm"],
+                                                     c["nsite"], Ls, 0)
+
+    ref = b5 * dw(phi) + phi + c5 * dw(chiv) - chiv
+    got = mob.mobius_m(c["U"], phi, c["nbr"], c["prm"], c["nsite"], Ls, b5, c5, M5, MF, 0)
+    assert rel_err(got, ref) < 1e-14
