@@ -45,6 +45,13 @@ LINK_BYTES = {0: 144, 1: 72, 2: 24, 3: 24}  # per link: F64, F32, 12-real F16/BF
 METRIC = "Dhop GFLOP/s & % HBM roofline; mixed vs plain CG time-to-1e-10 on 1 GB300"
 DIMS = (16, 16, 16, 16)
 LS = 16
+# The workload both arms name in `config` (identical dicts: the same lattice, precision and
+# working set; how each arm launches it is reported outside `config`).
+CONFIG = {"workload": "FP32 domain-wall Wilson Dhop, 16^4 x Ls=16, periodic", "lattice": list(DIMS), "Ls": LS,
+          "l2": "inputs larger than L2: two alternating in/out pairs, 476 MB vs 129 MB L2"}
+WHY_PORT = ("the oracle port stands in for the reference's dslash_simple.h (bit-identical to it on the same inputs, "
+            "checked where the reference tree exists); the reference tree is not present on the GPU host, and the "
+            "reference's AVX-512/AVX2 hand kernels are x86 intrinsics that do not build on its Arm cores")
 
 
 def algo_bytes(sprec: int, gprec: int, Ls: int, k: int = 1) -> float:
@@ -167,11 +174,10 @@ def ncu_traffic(key: str):
 def cpu_baseline(dims, Ls, budget_s=10.0) -> dict:
     """The oracle port (scalar C restatement of dslash_simple.h, OpenMP over all host
     threads) on the full FP32 lattice, repeated for about budget_s seconds."""
-    import gridbench_gb300 as gb
     import oracle
-    U = gb.generate_gauge(dims).astype(np.float32)
-    phi = gb.generate_fermion(dims, Ls).astype(np.float32)
-    nbr, prm, nsite = gb.generate_table(dims, Ls)
+    U = oracle.generate_gauge(dims).astype(np.float32)
+    phi = oracle.generate_fermion(dims, Ls).astype(np.float32)
+    nbr, prm, nsite = oracle.generate_table(dims, Ls)
     out = np.zeros_like(phi)
     oracle.dslash_sites(U, phi, out, nbr, 0, nsite, Ls)  # warm
     t = time.perf_counter()
@@ -200,7 +206,8 @@ def cpu_baseline(dims, Ls, budget_s=10.0) -> dict:
             "sample": f"{reps} full FP32 Dhop passes over {'x'.join(map(str, dims))} x Ls={Ls} "
                       f"({dt:.1f} s, oracle port of dslash_simple.h with OpenMP)",
             "single_thread": {"value": round(FLOP_PER_SITE * nsite * Ls * reps1 / dt1 / 1e9, 3), "cores": 1,
-                              "sample": f"{reps1} passes ({dt1:.1f} s)"}}
+                              "sample": f"{reps1} passes ({dt1:.1f} s)"},
+            "why_port": WHY_PORT}
 
 
 def time_dhop(gb, g, pairs, steps, warmup, dag=0):
@@ -220,13 +227,29 @@ def time_dhop(gb, g, pairs, steps, warmup, dag=0):
 
 
 def rel_to(gb, lat, a, b) -> float:
-    """|a - b| / |b| on the device in FP64."""
-    d = gb.Field(lat, gb.F64)
+    """|a - b| / |b| on the device in FP64 (every right-hand side of multi-RHS fields)."""
+    d = gb.Field(lat, gb.F64, a.nrhs)
     d.copy_from(a)
-    bb = gb.Field(lat, gb.F64)
+    bb = gb.Field(lat, gb.F64, b.nrhs)
     bb.copy_from(b)
     d.axpby(-1.0, bb, 1.0)
     return float(np.sqrt(d.norm2() / bb.norm2()))
+
+
+def halo_rel_err(x32, x64) -> float:
+    """Relative error of the eight FP32 halo faces of x32 against the same faces packed from
+    an FP64 field holding x32's values, over all faces (both packed to host memory and
+    decoded from the transport format: FP32 slice pairs (Re s, Re s+1, Im s, Im s+1), FP64
+    (Re, Im) per slice)."""
+    num = den = 0.0
+    for mu in range(4):
+        for face in (0, 1):
+            a = x32.halo_pack(mu, face).view(np.float32).reshape(-1, LS // 2, 2, 2)
+            a = a.transpose(0, 1, 3, 2).reshape(-1, LS, 2).astype(np.float64)  # (re/im pairs) -> (slice, re/im)
+            b = x64.halo_pack(mu, face).view(np.float64).reshape(-1, LS, 2)
+            num += float(np.sum((a - b) ** 2))
+            den += float(np.sum(b ** 2))
+    return float(np.sqrt(num / den))
 
 
 def measured_fp64_peak() -> dict | None:
@@ -311,11 +334,24 @@ def secondary(gb, args, peak) -> dict:
     for _ in range(steps):
         gb.dwf_m5inv(ze, ye, 1.8, 0.01)
     t5 = tm.stop() / steps / 1e3
+    # FP64 references on the same input values
+    ge64 = g64.checkerboard(le)
+    xo64, ye64, yy64, ze64 = gb.Field(lo, gb.F64), gb.Field(le, gb.F64), gb.Field(le, gb.F64), gb.Field(le, gb.F64)
+    xo64.copy_from(xo)
+    gb.dhop_eo(ge, ye, xo)
+    gb.dhop_eo(ge64, ye64, xo64)
+    eo_err = rel_to(gb, le, ye, ye64)
+    yy64.copy_from(ye)
+    gb.dwf_m5inv(ze, ye, 1.8, 0.01)
+    gb.dwf_m5inv(ze64, yy64, 1.8, 0.01)
+    m5_err = rel_to(gb, le, ze, ze64)
     out["dhop_eo_f32_16^4x16"] = {
         "gflops": round(FLOP_PER_SITE * V5 / 2 / t / 1e9, 1), "ms": round(t * 1e3, 4),
         "hbm_frac": round(algo_bytes(1, 1, LS) * V5 / 2 / t / 1e9 / peak, 3), "launch": list(gb.tune_query(g32, x32)),
-        "m5inv_ms": round(t5 * 1e3, 4), "m5inv_hbm_frac": round(2 * 96 * V5 / 2 / t5 / 1e9 / peak, 3)}
-    del ge, xo, ye, ze, le, lo
+        "rel_err_vs_fp64": eo_err,
+        "m5inv_ms": round(t5 * 1e3, 4), "m5inv_hbm_frac": round(2 * 96 * V5 / 2 / t5 / 1e9 / peak, 3),
+        "m5inv_rel_err_vs_fp64": m5_err}
+    del ge, xo, ye, ze, ge64, xo64, ye64, yy64, ze64, le, lo
     # Mobius (b = 1.5, c = 0.5): M = Mooee - 1/2 Dhop A(b, c) is one 5th-dimension pass and the
     # hopping pass with the Mooee epilogue; the 5th-dimension pass alone is HBM bound (one FP32
     # spinor read and one written per 5D site)
@@ -331,13 +367,24 @@ def secondary(gb, args, peak) -> dict:
         return tm.stop() / steps / 1e3
 
     tmob = per_call(lambda: gb.mobius_m(g32, y32, t32, x32, 1.5, 0.5, 1.8, 0.01))
+    # the same operator in FP64 on the same input (x64 holds the values x32 was rounded from;
+    # the FP64 reference takes x32's own values)
+    xr, yr, tr = gb.Field(lat, gb.F64), gb.Field(lat, gb.F64), gb.Field(lat, gb.F64)
+    xr.copy_from(x32)
+    gb.mobius_m(g32, y32, t32, x32, 1.5, 0.5, 1.8, 0.01)
+    gb.mobius_m(g64, yr, tr, xr, 1.5, 0.5, 1.8, 0.01)
+    mob_err = rel_to(gb, lat, y32, yr)
     tsham = per_call(lambda: gb.dwf_m(g32, y32, x32, 1.8, 0.01))
+    gb.dwf_m(g64, yr, xr, 1.8, 0.01)
+    gb.dwf_m(g32, y32, x32, 1.8, 0.01)
+    sham_err = rel_to(gb, lat, y32, yr)
     tm5d = per_call(lambda: gb.mobius_mooee(t32, x32, 1.5, 0.5, 1.8, 0.01))
     out["mobius_m_f32_16^4x16"] = {
         "ms": round(tmob * 1e3, 4), "shamir_m_ms": round(tsham * 1e3, 4),
         "m5d_ms": round(tm5d * 1e3, 4), "m5d_hbm_frac": round(2 * 96 * V5 / tm5d / 1e9 / peak, 3),
+        "rel_err_vs_fp64": mob_err, "shamir_m_rel_err_vs_fp64": sham_err,
         "b": 1.5, "c": 0.5, "M5": 1.8, "mf": 0.01}
-    del t32
+    del t32, tr
     # halo packing for a domain decomposition: the 8 faces' projected half spinors into device
     # buffers (allocated through torch, plumbing only); HBM bytes = every face spinor read once,
     # half of it written.  Four source fields rotate so the faces read (4 x 50 MB) exceed L2.
@@ -359,14 +406,15 @@ def secondary(gb, args, peak) -> dict:
         out["halo_pack_f32_16^4x16_8faces"] = {
             "us": round(thalo * 1e6, 2), "face_sites5": face5, "bytes": face5 * (96 + 48),
             "hbm_frac": round(face5 * (96 + 48) / thalo / 1e9 / peak, 3), "launches": 1,
+            "rel_err_vs_fp64": halo_rel_err(x32, xr),
             "l2": "four source fields rotate: 200 MB of faces read vs 129 MB L2"}
         del bufs, srcs
     except ImportError:
         pass
-    del g64, g32, g16, x64, y64, x32, y32, x16, y16, lat
+    del g64, g32, g16, x64, y64, x32, y32, x16, y16, xr, yr, lat
     if not args.quick:
         out["multi_rhs_24^4x12_k12"] = bench_mrhs(gb, peak)
-        out["batch_64"] = bench_batch(gb)
+        out["batch_64"] = bench_batch(gb, peak)
         out["cg_32^4x16"] = bench_cg(gb, args)
     return out
 
@@ -393,25 +441,34 @@ def bench_mrhs(gb, peak) -> dict:
     outs = [gb.Field(lat, gb.F32) for _ in range(2)]
     ms_single, _ = time_dhop(gb, g, [(outs[r % 2], singles[r]) for r in range(k)], 10 * k, k)
     t_single = ms_single / 10 / 1e3
-    # error of the 12-RHS result against single launches (rhs 0), through host export
+    # error of the 12-RHS result against single launches (rhs 0), through host export, and of
+    # all 12 against the FP64 hopping term of the same sources
     gb.dhop(g, Y, X)
     gb.dhop(g, y1, singles[0])
     err = float(np.linalg.norm(Y.numpy(0) - y1.numpy()) / np.linalg.norm(y1.numpy()))
+    del singles, outs
+    g64 = gb.Gauge(lat, None, gb.F64, seed=5)
+    X64, Y64 = gb.Field(lat, gb.F64, k), gb.Field(lat, gb.F64, k)
+    X64.copy_from(X)
+    gb.dhop(g64, Y64, X64)
+    err64 = rel_to(gb, lat, Y, Y64)
+    del g64, X64, Y64
     per_src_multi = FLOP_PER_SITE * V5 * k / t_multi / 1e9
     per_src_single = FLOP_PER_SITE * V5 * k / t_single / 1e9
     return {"gflops_12rhs": round(per_src_multi, 1), "gflops_12x1rhs": round(per_src_single, 1),
             "per_source_speedup": round(per_src_multi / per_src_single, 3),
             "byte_model_ceiling": round(algo_bytes(1, 1, Ls, 1) / algo_bytes(1, 1, Ls, k), 3),
             "hbm_frac_12rhs": round(algo_bytes(1, 1, Ls, k) * V5 * k / t_multi / 1e9 / peak, 3),
-            "rel_err_vs_single": err, "launch": list(gb.tune_query(g, X))}
+            "rel_err_vs_single": err, "rel_err_vs_fp64": err64, "launch": list(gb.tune_query(g, X))}
 
 
-def bench_batch(gb) -> dict:
+def bench_batch(gb, peak) -> dict:
     rng = np.random.default_rng(2024)
     vols = [8, 12, 16, 20, 24]
-    keep, G, O, I = [], [], [], []
+    keep, G, O, I, spec = [], [], [], [], []
     flops = 0
     sites5 = 0
+    nbytes = 0.0
     for k in range(64):
         L = int(rng.choice(vols))
         Ls = int(rng.choice([8, 12, 16]))
@@ -424,8 +481,11 @@ def bench_batch(gb) -> dict:
         G.append(g)
         O.append(y)
         I.append(x)
+        spec.append((L, Ls, prec))
         flops += FLOP_PER_SITE * L ** 4 * Ls
         sites5 += L ** 4 * Ls
+        sp = 1 if prec == gb.F32 else 2
+        nbytes += algo_bytes(sp, sp, Ls) * L ** 4 * Ls
     t0 = time.perf_counter()
     b = gb.Batch(G, O, I)
     tune_s = time.perf_counter() - t0
@@ -448,8 +508,21 @@ def bench_batch(gb) -> dict:
             gb.dhop(g, y, x)
     ms_sep = t.stop() / reps
     info = b.info()
+    # every instance against the FP64 hopping term of its own input values
+    b.run()
+    gb.synchronize()
+    errs = {gb.F32: 0.0, gb.F16: 0.0}
+    for k, (L, Ls, prec) in enumerate(spec):
+        g64 = gb.Gauge(keep[k], None, gb.F64, seed=1000 + k)
+        x64, y64 = gb.Field(keep[k], gb.F64), gb.Field(keep[k], gb.F64)
+        x64.copy_from(I[k])
+        gb.dhop(g64, y64, x64)
+        errs[prec] = max(errs[prec], rel_to(gb, keep[k], O[k], y64))
+        del g64, x64, y64
     return {"instances": 64, "sites5": sites5, "gflops": round(flops / (ms / 1e3) / 1e9, 1),
             "ms_per_replay": round(ms, 3), "ms_64_separate_launches": round(ms_sep, 3),
+            "hbm_frac": round(nbytes / (ms / 1e3) / 1e9 / peak, 3), "algorithmic_bytes": int(nbytes),
+            "rel_err_vs_fp64": {"fp32_max": errs[gb.F32], "fp16_max": errs[gb.F16]},
             "graph": info["graph"], "ctas": info["ctas"], "threads": info["threads"],
             "tune_seconds": round(tune_s, 2)}
 
@@ -615,14 +688,12 @@ def run_ours(args, D: Dist) -> dict | None:
         "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 5), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
         "data": "synthetic: seeded random SU(3) links (Gaussian -> Gram-Schmidt -> det 1), N(0,1) fermion",
-        "config": {"workload": "FP32 domain-wall Wilson Dhop, 16^4 x Ls=16, periodic", "lattice": list(DIMS),
-                   "Ls": LS, "parallelism": "replicas" if D.world > 1 else "single",
-                   "l2": "inputs larger than L2: two alternating in/out pairs, 476 MB vs 129 MB L2",
-                   "launch": {"threads": cfg[0], "slices_per_thread": cfg[1],
-                              "form": {0: "direct", 1: "tma-staged (CTA ring)", 2: "tma-staged (warp rings)",
-                                       3: "direct (Ls=16 specialised)",
-                                       4: "direct (Ls=16, 2^4 site blocks)"}[cfg[2]],
-                              "stages": cfg[3]}},
+        "config": dict(CONFIG),
+        "parallelism": "replicas" if D.world > 1 else "single",
+        "launch": {"threads": cfg[0], "slices_per_thread": cfg[1],
+                   "form": {0: "direct", 1: "tma-staged (CTA ring)", 2: "tma-staged (warp rings)",
+                            3: "direct (Ls=16 specialised)", 4: "direct (Ls=16, 2^4 site blocks)"}[cfg[2]],
+                   "stages": cfg[3]},
         "rel_err_vs_fp64": rel,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
@@ -645,18 +716,20 @@ def run_ours(args, D: Dist) -> dict | None:
 def run_reference(args, D: Dist) -> dict | None:
     """The reference's algorithm on the host CPU: the oracle port of dslash_simple.h (the
     reference's own kernels are x86-only and its tree is not present on the GPU host), all
-    host threads, each step a bounded sample of the 16^4 x Ls=16 FP32 workload."""
+    host threads, each step a bounded sample of the 16^4 x Ls=16 FP32 workload.  Inputs come
+    from the oracle's own generator: this arm never loads the product library.  Like our arm
+    it alternates two in/out pairs."""
     if D.rank != 0:
         return None
-    import gridbench_gb300 as gb
     import oracle
-    U = gb.generate_gauge(DIMS).astype(np.float32)
-    phi = gb.generate_fermion(DIMS, LS).astype(np.float32)
-    nbr, prm, nsite = gb.generate_table(DIMS, LS)
-    out = np.zeros_like(phi)
-    oracle.dslash_sites(U, phi, out, nbr, 0, nsite, LS)
+    U = oracle.generate_gauge(DIMS).astype(np.float32)
+    phis = [oracle.generate_fermion(DIMS, LS).astype(np.float32),
+            oracle.generate_fermion(DIMS, LS, 1, (9, 10, 11, 12)).astype(np.float32)]
+    nbr, prm, nsite = oracle.generate_table(DIMS, LS)
+    outs = [np.zeros_like(phis[0]) for _ in range(2)]
+    oracle.dslash_sites(U, phis[0], outs[0], nbr, 0, nsite, LS)
     t = time.perf_counter()
-    oracle.dslash_sites(U, phi, out, nbr, 0, nsite, LS)
+    oracle.dslash_sites(U, phis[0], outs[0], nbr, 0, nsite, LS)
     t_full = time.perf_counter() - t
     budget = args.ref_seconds
     per_step = budget / max(1, args.steps + args.warmup)
@@ -664,11 +737,11 @@ def run_reference(args, D: Dist) -> dict | None:
     sample = max(64, int(nsite * frac))
     sample = min(sample, nsite)
     for i in range(args.warmup):
-        oracle.dslash_sites(U, phi, out, nbr, 0, sample, LS)
+        oracle.dslash_sites(U, phis[i % 2], outs[i % 2], nbr, 0, sample, LS)
     t = time.perf_counter()
     for i in range(args.steps):
         s0 = (i * sample) % (nsite - sample + 1)
-        oracle.dslash_sites(U, phi, out, nbr, s0, s0 + sample, LS)
+        oracle.dslash_sites(U, phis[i % 2], outs[i % 2], nbr, s0, s0 + sample, LS)
     dt = time.perf_counter() - t
     value = FLOP_PER_SITE * sample * LS * args.steps / dt / 1e9
     desc = (f"each step: {sample} of {nsite} 4D sites (x Ls={LS}) of the 16^4 FP32 lattice, "
@@ -676,11 +749,10 @@ def run_reference(args, D: Dist) -> dict | None:
     return {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GFLOP/s", "n_gpus": D.world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
-            "data": "synthetic: seeded random SU(3) links, N(0,1) fermion",
-            "config": {"workload": "FP32 domain-wall Wilson Dhop, 16^4 x Ls=16, periodic", "lattice": list(DIMS),
-                       "Ls": LS, "l2": "host CPU run"},
+            "data": "synthetic: seeded random SU(3) links (Gaussian -> Gram-Schmidt -> det 1), N(0,1) fermion",
+            "config": dict(CONFIG),
             "cpu_baseline": {"value": round(value, 3), "unit": "GFLOP/s", "cores": oracle.threads(), "kind": "port",
-                             "sample": desc},
+                             "sample": desc, "why_port": WHY_PORT},
             "e2e": {"value": round(value, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 

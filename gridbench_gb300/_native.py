@@ -126,6 +126,7 @@ PROTOTYPES = {
     "gbdw_timer_destroy": (_i, [_vp]),
     "gbdw_flush_l2": (_i, [C.c_size_t]),
     "gbdw_norm2_noalloc": (_i, [_vp, _i, _u64, _dp]),
+    "gbdw_debug_fail_allocs": (_i, [_i, _i]),
     "gbdw_host_alloc": (_i, [C.c_size_t, _pp]),
     "gbdw_host_free": (_i, [_vp]),
 }

@@ -263,8 +263,8 @@ int gbdw_batch_create(gbdw_batch** out, int n, const gbdw_gauge* const* gauges, 
   b->out.assign(outs, outs + n);
   b->in.assign(ins, ins + n);
   b->dag = dag ? 1 : 0;
-  cudaError_t e = cudaMalloc(&b->d_inst, sizeof(BatchInst) * n);
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_next, 64);
+  cudaError_t e = dev_alloc((void**)&b->d_inst, sizeof(BatchInst) * n);
+  if (e == cudaSuccess) e = dev_alloc((void**)&b->d_next, 64);
   if (e != cudaSuccess) {
     if (b->d_inst) cudaFree(b->d_inst);
     delete b;

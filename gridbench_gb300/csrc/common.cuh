@@ -29,6 +29,10 @@ void count_launch(uint64_t n = 1);
 void* scratch(size_t bytes, int slot);
 int ensure_device();
 int num_sms();
+// Device the library's stream belongs to (-1 before the first ensure_device()).
+int library_device();
+// cudaMalloc through the library's one allocation point (honours gbdw_debug_fail_allocs).
+cudaError_t dev_alloc(void** p, size_t bytes);
 unsigned* device_error_word();  // set by kernels whose bounded waits expired
 size_t max_dynamic_smem();      // opt-in dynamic shared memory per CTA, minus room for static
 

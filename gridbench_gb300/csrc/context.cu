@@ -18,7 +18,12 @@ cudaStream_t g_user_stream = nullptr;
 cudaStream_t g_own_stream = nullptr;
 bool g_have_user_stream = false;
 int g_device_checked = 0;  // 0 unknown, 1 ok, -1 none
+int g_device = -1;         // the device current when the library first ran (its stream lives there)
 int g_num_sms = 0;
+// Host-side allocation-failure injection (gbdw_debug_fail_allocs): skip this many more
+// device allocations, then fail this many.
+std::atomic<long> g_alloc_skip{0};
+std::atomic<long> g_alloc_fail{0};
 
 struct ScratchSlot {
   void* p = nullptr;
@@ -62,6 +67,7 @@ int ensure_device() {
   int dev = 0;
   GBDW_CUDA(cudaGetDevice(&dev));
   GBDW_CUDA(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
+  g_device = dev;
   if (!g_own_stream) GBDW_CUDA(cudaStreamCreateWithFlags(&g_own_stream, cudaStreamNonBlocking));
   if (!g_pinned) GBDW_CUDA(cudaMallocHost((void**)&g_pinned, 64 * sizeof(double)));
   g_device_checked = 1;
@@ -69,6 +75,21 @@ int ensure_device() {
 }
 
 int num_sms() { return g_num_sms > 0 ? g_num_sms : 152; }
+
+int library_device() { return g_device; }
+
+cudaError_t dev_alloc(void** p, size_t bytes) {
+  if (g_alloc_fail.load() > 0) {
+    if (g_alloc_skip.load() > 0) {
+      --g_alloc_skip;
+    } else {
+      --g_alloc_fail;
+      *p = nullptr;
+      return cudaErrorMemoryAllocation;  // as cudaMalloc reports an exhausted device
+    }
+  }
+  return cudaMalloc(p, bytes);
+}
 
 size_t max_dynamic_smem() {
   static size_t v = 0;
@@ -99,7 +120,7 @@ void* scratch(size_t bytes, int slot) {
     s.bytes = 0;
   }
   size_t want = bytes < (1u << 20) ? (1u << 20) : bytes;
-  if (cudaMalloc(&s.p, want) != cudaSuccess) {
+  if (dev_alloc(&s.p, want) != cudaSuccess) {
     cudaGetLastError();
     s.p = nullptr;
     return nullptr;
@@ -294,6 +315,17 @@ int gbdw_host_alloc(size_t nbytes, void** ptr) {
   if (!ptr || nbytes == 0) return GBDW_ERR_INVALID;
   if (int st = ensure_device()) return st;
   GBDW_CUDA(cudaMallocHost(ptr, nbytes));
+  return GBDW_OK;
+}
+
+int gbdw_debug_fail_allocs(int skip, int count) {
+  if (skip < 0 || count < 0) {
+    set_error("gbdw_debug_fail_allocs: skip and count must be >= 0");
+    return GBDW_ERR_INVALID;
+  }
+  g_alloc_fail = 0;
+  g_alloc_skip = skip;
+  g_alloc_fail = count;
   return GBDW_OK;
 }
 

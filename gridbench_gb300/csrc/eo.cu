@@ -391,8 +391,8 @@ int gbdw_lattice_checkerboard(const gbdw_lattice* full, gbdw_lattice** even, gbd
     L->fast = true;
     L->parity = par;
     L->parent = full;
-    cudaError_t e = cudaMalloc(&L->nbr4, size_t(nh) * 8 * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&L->cbsite, size_t(nh) * sizeof(uint32_t));
+    cudaError_t e = dev_alloc((void**)&L->nbr4, size_t(nh) * 8 * sizeof(uint32_t));
+    if (e == cudaSuccess) e = dev_alloc((void**)&L->cbsite, size_t(nh) * sizeof(uint32_t));
     if (e != cudaSuccess) {
       gbdw_lattice_destroy(L);
       if (H[0]) gbdw_lattice_destroy(H[0]);
@@ -425,7 +425,7 @@ int gbdw_gauge_checkerboard(gbdw_gauge** out, const gbdw_gauge* full, const gbdw
   G->lat = half;
   G->prec = full->prec;
   G->bytes = size_t(half->nsite) * 8 * link_bytes(full->prec);
-  cudaError_t e = cudaMalloc(&G->d, G->bytes);
+  cudaError_t e = dev_alloc((void**)&G->d, G->bytes);
   if (e != cudaSuccess) {
     delete G;
     return cuda_fail(e, "cudaMalloc(half gauge)");

@@ -345,7 +345,7 @@ int lattice_from_table_impl(gbdw_lattice** out, uint64_t nouter, int Ls, int nsi
     delete L;
     return st;
   };
-  cudaError_t e = cudaMalloc(&L->nbr4, size_t(L->nsite) * 8 * sizeof(uint32_t));
+  cudaError_t e = dev_alloc((void**)&L->nbr4, size_t(L->nsite) * 8 * sizeof(uint32_t));
   if (e != cudaSuccess) return fail(cuda_fail(e, "cudaMalloc(nbr4)"));
   if ((e = cudaMemsetAsync(dflags, 0, sizeof(unsigned), stream())) != cudaSuccess) return fail(cuda_fail(e, "memset"));
   k_table_check<<<nblk(nent, 256), 256, 0, stream()>>>((const uint64_t*)dnbr, (const uint8_t*)dprm, int64_t(nouter), Ls,
@@ -362,7 +362,7 @@ int lattice_from_table_impl(gbdw_lattice** out, uint64_t nouter, int Ls, int nsi
   }
   L->fast = !(flags & 2u) && !force_general;
   if (!L->fast) {
-    e = cudaMalloc(&L->nbr5, size_t(L->nsite) * Ls * 8 * sizeof(uint32_t));
+    e = dev_alloc((void**)&L->nbr5, size_t(L->nsite) * Ls * 8 * sizeof(uint32_t));
     if (e != cudaSuccess) return fail(cuda_fail(e, "cudaMalloc(nbr5)"));
     k_table_general<<<nblk(nent, 256), 256, 0, stream()>>>((const uint64_t*)dnbr, (const uint8_t*)dprm, int64_t(nouter),
                                                             Ls, nsimd, L->nbr5);
@@ -410,7 +410,7 @@ int gbdw_lattice_create(gbdw_lattice** lat, const int dims[4], int Ls) {
   L->fast = true;
   L->nbr5 = nullptr;
   for (int d = 0; d < 4; ++d) L->dims[d] = dims[d];
-  cudaError_t e = cudaMalloc(&L->nbr4, size_t(V) * 8 * sizeof(uint32_t));
+  cudaError_t e = dev_alloc((void**)&L->nbr4, size_t(V) * 8 * sizeof(uint32_t));
   if (e != cudaSuccess) {
     delete L;
     return cuda_fail(e, "cudaMalloc(nbr4)");
@@ -459,7 +459,7 @@ int gbdw_gauge_create(gbdw_gauge** g, const gbdw_lattice* lat, int prec, const v
   G->lat = lat;
   G->prec = prec;
   G->bytes = size_t(nlink) * link_bytes(prec);
-  cudaError_t e = cudaMalloc(&G->d, G->bytes);
+  cudaError_t e = dev_alloc((void**)&G->d, G->bytes);
   if (e != cudaSuccess) {
     delete G;
     return cuda_fail(e, "cudaMalloc(gauge)");
@@ -520,13 +520,13 @@ int gbdw_field_create(gbdw_field** f, const gbdw_lattice* lat, int prec, int nrh
   F->LsP = padded_slices(prec, F->LsE);
   F->norm = nullptr;
   F->bytes = size_t(F->elems()) * spinor_elem_bytes(prec);
-  cudaError_t e = cudaMalloc(&F->d, F->bytes);
+  cudaError_t e = dev_alloc((void**)&F->d, F->bytes);
   if (e != cudaSuccess) {
     delete F;
     return cuda_fail(e, "cudaMalloc(field)");
   }
   if (prec == GBDW_F16) {
-    e = cudaMalloc(&F->norm, size_t(lat->nsite) * F->LsE * sizeof(float));
+    e = dev_alloc((void**)&F->norm, size_t(lat->nsite) * F->LsE * sizeof(float));
     if (e != cudaSuccess) {
       cudaFree(F->d);
       delete F;

@@ -161,7 +161,7 @@ int gbdw_gauge_random(gbdw_gauge** g, const gbdw_lattice* lat, int prec, uint64_
   G->lat = lat;
   G->prec = prec;
   G->bytes = size_t(nsite) * 8 * link_bytes(prec);
-  cudaError_t e = cudaMalloc(&G->d, G->bytes);
+  cudaError_t e = dev_alloc((void**)&G->d, G->bytes);
   if (e != cudaSuccess) {
     delete G;
     return cuda_fail(e, "cudaMalloc(gauge)");

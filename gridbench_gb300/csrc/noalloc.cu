@@ -19,8 +19,16 @@
 //    The counter is cleared at the start of every call, so a call never depends on what an
 //    earlier call left behind.
 //  - the first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (once per device, with that device current); make that first call
-//    before any stream capture.
+//    cudaGetSymbolAddress (once per device, with that device current);
+//  - every call is synchronous: it ends with a copy of the result into host memory and a
+//    synchronisation of the library's stream, so no call may be made while a stream is being
+//    captured into a CUDA graph;
+//  - the kernel runs on the library's stream (gbdw_set_stream selects it), so x must be
+//    complete with respect to that stream: a caller that wrote x on another stream
+//    synchronises that stream first or hands it to gbdw_set_stream;
+//  - like the rest of the library it works on one device, the one current when the library
+//    first ran (its stream lives there); once the library has run, a call made with another
+//    device current is rejected.
 #include <mutex>
 
 #include "common.cuh"
@@ -90,6 +98,15 @@ extern "C" int gbdw_norm2_noalloc(const void* x, int prec, uint64_t n, double* r
   if (n == 0) {
     *result = 0.0;
     return GBDW_OK;
+  }
+  // no ensure_device() here: its first run allocates (the library's stream and pinned
+  // staging); before any other library call the work goes to the legacy default stream
+  int dev = 0;
+  GBDW_CUDA(cudaGetDevice(&dev));
+  if (library_device() >= 0 && dev != library_device()) {
+    set_error("gbdw_norm2_noalloc: device " + std::to_string(dev) + " is current, but the library runs on device " +
+              std::to_string(library_device()) + " (its stream lives there)");
+    return GBDW_ERR_INVALID;
   }
   double* scratch = nullptr;
   if (int st = scratch_address(&scratch)) return st;

@@ -371,9 +371,21 @@ int gbdw_selftest_wait_timeout(uint64_t limit_ns);
  * in a fixed 8 KB device array that every GPU loading the library keeps until exit.  No
  * counterpart in the reference.  Limit: n <= 2^24 (larger n returns GBDW_ERR_INVALID).  All
  * calls share that array, so calls that overlap on the GPU race; calls in one stream do not.
- * The first call on each device looks the array up (cudaGetSymbolAddress): make it before
- * any stream capture. */
+ * The first call on each device looks the array up (cudaGetSymbolAddress).  The call is
+ * synchronous (it copies the result to the host and waits for the library's stream), so it
+ * must not be made while any stream is being captured into a CUDA graph.  It reads x on the
+ * library's stream: x must be complete with respect to that stream (synchronise the stream
+ * that wrote x first, or make it the library's stream with gbdw_set_stream).  Single device,
+ * like the rest of the library: once the library has run, a call made with a device current
+ * other than the one it first ran on returns GBDW_ERR_INVALID. */
 int gbdw_norm2_noalloc(const void* x, int prec, uint64_t n, double* result);
+
+/* Host-side fault injection for tests (no counterpart in the reference; GridBench exits on
+ * any CUDA error, Macros.h:47-51): after `skip` more device allocations made by the library,
+ * the next `count` fail exactly as an exhausted device makes cudaMalloc fail, so the caller
+ * sees GBDW_ERR_ALLOC; later allocations succeed again.  count = 0 switches injection off.
+ * No kernel is involved: the GPU never faults. */
+int gbdw_debug_fail_allocs(int skip, int count);
 
 /* Page-locked host memory for fast host<->device copies of reference-layout buffers. */
 int gbdw_host_alloc(size_t nbytes, void** ptr);

@@ -43,11 +43,60 @@ def lib():
             f = getattr(L, "or_dwf_m" + sfx)
             f.argtypes = [rp, rp, rp, _u64p, C.c_uint64, C.c_uint64, C.c_double, C.c_double, C.c_int]
             f.restype = None
+        L.or_seed_from_ints.argtypes = [C.c_void_p, C.c_int]
+        L.or_seed_from_ints.restype = C.c_uint64
+        L.or_generate_gauge.argtypes = [C.c_void_p, C.c_int, C.c_uint64, _f64p]
+        L.or_generate_fermion.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_uint64, _f64p]
+        L.or_generate_table.argtypes = [C.c_void_p, C.c_int, C.c_int, _u64p, _u8p]
+        for n in ("or_generate_gauge", "or_generate_fermion", "or_generate_table"):
+            getattr(L, n).restype = C.c_int
         L.or_set_threads.argtypes = [C.c_int]
         L.or_set_threads.restype = None
         L.or_max_threads.restype = C.c_int
         _lib = L
     return _lib
+
+
+def _dims(dims) -> np.ndarray:
+    d = np.ascontiguousarray(dims, dtype=np.int32)
+    if d.shape != (4,):
+        raise ValueError("dims must have 4 entries (Lx, Ly, Lz, Lt)")
+    return d
+
+
+def seed_from_ints(seeds) -> int:
+    a = np.ascontiguousarray(seeds, dtype=np.int32)
+    return int(lib().or_seed_from_ints(C.c_void_p(a.ctypes.data), len(a)))
+
+
+def generate_gauge(dims, nsimd: int = 1, seeds=(1, 2, 3, 4)) -> np.ndarray:
+    """Doubled random SU(3) field in the reference layout, FP64 (the oracle's own generator,
+    bit-identical to the product's; TableGenerate.cc:44,54 plays this role for GridBench)."""
+    d = _dims(dims)
+    U = np.empty(int(np.prod(d)) * 8 * 9 * 2, dtype=np.float64)
+    if lib().or_generate_gauge(C.c_void_p(d.ctypes.data), nsimd, seed_from_ints(seeds), U):
+        raise ValueError("bad dims / nsimd")
+    return U
+
+
+def generate_fermion(dims, Ls: int, nsimd: int = 1, seeds=(5, 6, 7, 8)) -> np.ndarray:
+    """Gaussian 5D fermion in the reference layout, FP64 (TableGenerate.cc:36's role)."""
+    d = _dims(dims)
+    phi = np.empty(int(np.prod(d)) * Ls * 24, dtype=np.float64)
+    if lib().or_generate_fermion(C.c_void_p(d.ctypes.data), Ls, nsimd, seed_from_ints(seeds), phi):
+        raise ValueError("bad dims / Ls / nsimd")
+    return phi
+
+
+def generate_table(dims, Ls: int, nsimd: int = 1):
+    """nbr/prm stencil tables (TableGenerate.cc:75-91); returns (nbr, prm, nsite)."""
+    d = _dims(dims)
+    nsite = int(np.prod(d)) // nsimd
+    nbr = np.empty(nsite * Ls * 8, dtype=np.uint64)
+    prm = np.empty(nsite * Ls * 8, dtype=np.uint8)
+    if lib().or_generate_table(C.c_void_p(d.ctypes.data), Ls, nsimd, nbr, prm):
+        raise ValueError("bad dims / Ls / nsimd")
+    return nbr, prm, nsite
 
 
 def _sfx(a):

@@ -1,6 +1,7 @@
 """ORACLE build recipe (test infrastructure only).
 
-  liboracle.so      the C restatement (oracle.c), gcc, no FP contraction, OpenMP
+  liboracle.so      the C restatement (oracle.c) and the seeded input generator (gen.c), gcc,
+                    no FP contraction, OpenMP
   _ref/libref_dslash.so
                     GridBench's own dslash_simple.h compiled in place from the reference
                     tree through ref_shim.cc (only where that tree exists)
@@ -36,10 +37,10 @@ def _stale(target, deps):
 
 
 def build_oracle() -> str:
-    deps = [os.path.join(HERE, f) for f in ("oracle.c", "oracle_body.h")]
+    deps = [os.path.join(HERE, f) for f in ("oracle.c", "gen.c", "oracle_body.h")]
     if _stale(LIB, deps):
         _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
-              deps[0], "-o", LIB, "-lm"])
+              deps[0], deps[1], "-o", LIB, "-lm"])
     return LIB
 
 

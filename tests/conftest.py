@@ -41,3 +41,31 @@ def gpu():
     if not gb.device_available():
         pytest.fail("gpu-marked test but no CUDA device is visible: " + gb.load().gbdw_last_error().decode())
     return gb
+
+
+def host_memory_available() -> float:
+    """Bytes this process may still allocate on the host: MemAvailable, capped by the cgroup
+    limit when one is set (the big-lattice parity tests check it before they start)."""
+    avail = float("inf")
+    try:
+        for line in open("/proc/meminfo"):
+            if line.startswith("MemAvailable:"):
+                avail = float(line.split()[1]) * 1024
+    except OSError:
+        pass
+    for lim, cur in (("/sys/fs/cgroup/memory.max", "/sys/fs/cgroup/memory.current"),
+                     ("/sys/fs/cgroup/memory/memory.limit_in_bytes", "/sys/fs/cgroup/memory/memory.usage_in_bytes")):
+        try:
+            raw = open(lim).read().strip()
+            if raw != "max" and float(raw) < 1e18:
+                avail = min(avail, float(raw) - float(open(cur).read().strip()))
+            break
+        except (OSError, ValueError):
+            continue
+    return avail
+
+
+def need_host_memory(nbytes: float):
+    have = host_memory_available()
+    if have < nbytes:
+        pytest.skip(f"needs {nbytes / 2**30:.1f} GiB of host memory, {have / 2**30:.1f} GiB available")

@@ -117,3 +117,12 @@ def test_struct_layouts_match_the_header():
         assert int(out[cname]) == C.sizeof(py), cname
         for f, _ in py._fields_:
             assert int(out[f"{cname}.{f}"]) == getattr(py, f).offset, (cname, f)
+
+
+def test_allocation_failure_injection_argument_checks():
+    """The host-side injection hook needs no device: negative counts are refused, and
+    count = 0 switches injection off."""
+    L = gb.load()
+    assert L.gbdw_debug_fail_allocs(-1, 1) == _native.ERR_INVALID
+    assert L.gbdw_debug_fail_allocs(0, -2) == _native.ERR_INVALID
+    assert L.gbdw_debug_fail_allocs(0, 0) == _native.OK

@@ -82,3 +82,35 @@ def test_generator_rejects_bad_dims():
         gb.generate_gauge((3, 4, 4, 4), nsimd=16)  # x not divisible by its lane split
     with pytest.raises(gb.GbdwError):
         gb.generate_table((4, 4, 4, 4), 2, nsimd=3)
+
+
+def _oracle_case(dims, Ls, nsimd=1):
+    import oracle
+    nbr, prm, nsite = oracle.generate_table(dims, Ls, nsimd)
+    return {"U": oracle.generate_gauge(dims, nsimd), "phi": oracle.generate_fermion(dims, Ls, nsimd), "nbr": nbr,
+            "prm": prm, "nsite": nsite}
+
+
+@pytest.mark.parametrize("dims,Ls,nsimd", [((4, 4, 4, 4), 4, 1), ((4, 6, 2, 4), 3, 1), ((8, 8, 8, 8), 8, 4),
+                                           ((4, 4, 4, 8), 2, 16), ((2, 4, 4, 4), 3, 8), ((6, 2, 2, 10), 1, 2)])
+def test_oracle_generator_is_bit_identical_to_product(dims, Ls, nsimd):
+    """The oracle's own generator (oracle/gen.c, used by the reference-side CPU runs so they
+    never load the product library) and the product's gbdw_generate_* give the same bits."""
+    a = _oracle_case(dims, Ls, nsimd)
+    b = make_case(dims, Ls, nsimd)
+    for k in ("U", "phi", "nbr", "prm"):
+        assert np.ascontiguousarray(a[k]).tobytes() == np.ascontiguousarray(b[k]).tobytes(), k
+    assert a["nsite"] == b["nsite"]
+
+
+def test_oracle_generator_reproduces_golden_inputs():
+    import oracle
+    for f in sorted(glob.glob(os.path.join(GOLDEN, "golden_*.npz"))):
+        g = np.load(f)
+        c = _oracle_case(tuple(g["dims"]), int(g["Ls"]), int(g["nsimd"]))
+        for k in ("U", "phi", "nbr", "prm"):
+            if "sha_" + k in g:
+                assert hashlib.sha256(np.ascontiguousarray(c[k]).tobytes()).hexdigest() == str(g["sha_" + k]), (f, k)
+    assert oracle.seed_from_ints((1, 2, 3, 4)) == gb.seed_from_ints((1, 2, 3, 4))
+    with pytest.raises(ValueError):
+        oracle.generate_gauge((3, 4, 4, 4), nsimd=16)
