@@ -415,6 +415,7 @@ def secondary(gb, args, peak) -> dict:
     if not args.quick:
         out["multi_rhs_24^4x12_k12"] = bench_mrhs(gb, peak)
         out["batch_64"] = bench_batch(gb, peak)
+        out["batch_64_rhs_1_2_4"] = bench_batch(gb, peak, (1, 2, 4), seed=2025)
         out["cg_32^4x16"] = bench_cg(gb, args)
     return out
 
@@ -462,8 +463,12 @@ def bench_mrhs(gb, peak) -> dict:
             "rel_err_vs_single": err, "rel_err_vs_fp64": err64, "launch": list(gb.tune_query(g, X))}
 
 
-def bench_batch(gb, peak) -> dict:
-    rng = np.random.default_rng(2024)
+def bench_batch(gb, peak, nrhs_choices=(1,), seed=2024) -> dict:
+    """64 instances in one persistent launch replayed from a CUDA graph: 4D volumes uniform over
+    {8^4 .. 24^4}, Ls over {8, 12, 16}, FP32 or FP16 storage, right-hand sides from
+    nrhs_choices; against the same instances as 64 separate launches, each on its own
+    autotuned shape."""
+    rng = np.random.default_rng(seed)
     vols = [8, 12, 16, 20, 24]
     keep, G, O, I, spec = [], [], [], [], []
     flops = 0
@@ -473,19 +478,22 @@ def bench_batch(gb, peak) -> dict:
         L = int(rng.choice(vols))
         Ls = int(rng.choice([8, 12, 16]))
         prec = gb.F32 if rng.random() < 0.5 else gb.F16
+        nrhs = int(rng.choice(nrhs_choices))
         lat = gb.Lattice.periodic((L, L, L, L), Ls)
         g = gb.Gauge(lat, None, prec, seed=1000 + k)
-        x = gb.Field(lat, prec).gaussian(2000 + k)
-        y = gb.Field(lat, prec)
+        x = gb.Field(lat, prec, nrhs)
+        for r in range(nrhs):
+            x.gaussian(2000 + 97 * k + r, r)
+        y = gb.Field(lat, prec, nrhs)
         keep.append(lat)
         G.append(g)
         O.append(y)
         I.append(x)
-        spec.append((L, Ls, prec))
-        flops += FLOP_PER_SITE * L ** 4 * Ls
-        sites5 += L ** 4 * Ls
+        spec.append((L, Ls, prec, nrhs))
+        flops += FLOP_PER_SITE * L ** 4 * Ls * nrhs
+        sites5 += L ** 4 * Ls * nrhs
         sp = 1 if prec == gb.F32 else 2
-        nbytes += algo_bytes(sp, sp, Ls) * L ** 4 * Ls
+        nbytes += algo_bytes(sp, sp, Ls, nrhs) * L ** 4 * Ls * nrhs
     t0 = time.perf_counter()
     b = gb.Batch(G, O, I)
     tune_s = time.perf_counter() - t0
@@ -498,7 +506,12 @@ def bench_batch(gb, peak) -> dict:
     for _ in range(reps):
         b.run()
     ms = t.stop() / reps
-    # the same instances as 64 separate (tuned) launches
+    # the same instances as 64 separate launches, each (precision, Ls*nrhs) on its tuned shape
+    tuned = set()
+    for g, y, x, (L, Ls, prec, nrhs) in zip(G, O, I, spec):
+        if (prec, Ls * nrhs) not in tuned:
+            gb.tune_dhop(g, y, x)
+            tuned.add((prec, Ls * nrhs))
     for g, y, x in zip(G, O, I):
         gb.dhop(g, y, x)
     gb.synchronize()
@@ -512,18 +525,21 @@ def bench_batch(gb, peak) -> dict:
     b.run()
     gb.synchronize()
     errs = {gb.F32: 0.0, gb.F16: 0.0}
-    for k, (L, Ls, prec) in enumerate(spec):
+    for k, (L, Ls, prec, nrhs) in enumerate(spec):
         g64 = gb.Gauge(keep[k], None, gb.F64, seed=1000 + k)
-        x64, y64 = gb.Field(keep[k], gb.F64), gb.Field(keep[k], gb.F64)
+        x64, y64 = gb.Field(keep[k], gb.F64, nrhs), gb.Field(keep[k], gb.F64, nrhs)
         x64.copy_from(I[k])
         gb.dhop(g64, y64, x64)
         errs[prec] = max(errs[prec], rel_to(gb, keep[k], O[k], y64))
         del g64, x64, y64
-    return {"instances": 64, "sites5": sites5, "gflops": round(flops / (ms / 1e3) / 1e9, 1),
+    return {"instances": 64, "rhs_choices": list(nrhs_choices), "sites5": sites5,
+            "gflops": round(flops / (ms / 1e3) / 1e9, 1),
             "ms_per_replay": round(ms, 3), "ms_64_separate_launches": round(ms_sep, 3),
+            "speedup_vs_separate": round(ms_sep / ms, 3),
             "hbm_frac": round(nbytes / (ms / 1e3) / 1e9 / peak, 3), "algorithmic_bytes": int(nbytes),
             "rel_err_vs_fp64": {"fp32_max": errs[gb.F32], "fp16_max": errs[gb.F16]},
             "graph": info["graph"], "ctas": info["ctas"], "threads": info["threads"],
+            "shape": {"spt_f32": info["spt_f32"], "spt_f16": info["spt_f16"], "tile_split": info["tile_split"]},
             "tune_seconds": round(tune_s, 2)}
 
 

@@ -461,10 +461,17 @@ class Batch(_Handle):
     def run(self):
         check(load().gbdw_batch_run(self.h))
 
+    def set_shape(self, threads: int, spt_f32: int, spt_f16: int, split: int):
+        """Pins the launch shape and the tile split (rebuilds the graph)."""
+        check(load().gbdw_batch_set_shape(self.h, (C.c_int * 4)(threads, spt_f32, spt_f16, split)))
+
     def info(self) -> dict:
         a = (C.c_int64 * 4)()
         check(load().gbdw_batch_info(self.h, a))
-        return {"items": a[0], "ctas": a[1], "threads": a[2], "graph": bool(a[3])}
+        s = (C.c_int * 4)()
+        check(load().gbdw_batch_shape(self.h, s))
+        return {"items": a[0], "ctas": a[1], "threads": a[2], "graph": bool(a[3]), "spt_f32": s[1], "spt_f16": s[2],
+                "tile_split": s[3]}
 
 
 def tune_dhop(g: Gauge, out: Field, inp: Field, dag: int = 0) -> tuple:

@@ -114,6 +114,8 @@ PROTOTYPES = {
     "gbdw_batch_run": (_i, [_vp]),
     "gbdw_batch_destroy": (_i, [_vp]),
     "gbdw_batch_info": (_i, [_vp, _i64a]),
+    "gbdw_batch_shape": (_i, [_vp, C.POINTER(C.c_int)]),
+    "gbdw_batch_set_shape": (_i, [_vp, C.POINTER(C.c_int)]),
     "gbdw_tune_dhop": (_i, [_vp, _vp, _vp, _i]),
     "gbdw_tune_load": (_i, [C.c_char_p]),
     "gbdw_tune_save": (_i, [C.c_char_p]),

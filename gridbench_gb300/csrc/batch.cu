@@ -2,13 +2,27 @@
 // right-hand sides, gauge field and storage precision FP32 or FP16) applied in ONE
 // persistent launch that is captured once in a CUDA graph and replayed.
 //
-// The instances are cut into work items of one CTA's worth of threads (a thread owns
-// `spt` consecutive innermost slices of one site).  A grid of (SMs x resident CTAs per SM)
-// CTAs pulls items from a device counter with atomicAdd until the list is exhausted, so
-// uneven volumes balance dynamically; the loop is bounded by the item count and never
-// waits on another CTA.  The counter is reset by a memset node in the same graph.
-// Launch shape (threads per CTA, slices per thread for each precision) is chosen by timing
-// graph replays of the caller's own batch.
+// Work decomposition.  A thread owns `spt` consecutive innermost slices (e = s*nrhs + rhs)
+// of one site; the slices of a site are cut into `split` contiguous tiles of TE = LsE/split
+// slices, so a tile holds TE/nrhs values of s with all right-hand sides (an Ls tile) or, when
+// TE < nrhs, TE of the right-hand sides at one s (an RHS tile).  Threads are ordered (tile,
+// site, slice group), and an instance's threads are cut into work items of one CTA each.  The
+// link of a (site, leg) is loaded once per thread group and reused over its tile's slices;
+// more tiles put more sites in a CTA.
+//
+// Scheduling.  A grid of (SMs x resident CTAs per SM) CTAs pulls items from a device counter;
+// each CTA claims its next item while it works on the current one, so the atomic's latency is
+// hidden and uneven volumes still balance dynamically.  Items run largest instance first.
+// The loop is bounded by the item count and never waits on another CTA.  A memset node in the
+// same graph resets the counter.
+//
+// Kernels.  Rows of 8, 12 or 16 slots (Ls = 8/12/16 with one right-hand side) take a path with
+// the row stride a compile-time constant, as the single-instance specialised form does; other
+// extents take the runtime-stride path.  Registers are capped so that (threads x CTAs per SM)
+// ~ 384 threads stay resident, the operating point of the single-instance kernels.
+//
+// Tuning.  The shape (threads per CTA, slices per thread for FP32 and FP16 instances, tile
+// split) is chosen by timing graph replays of the caller's own batch.
 #include <algorithm>
 #include <vector>
 
@@ -20,60 +34,76 @@ namespace {
 
 struct BatchInst {
   DhopParams p;
-  unsigned item_begin;
-  unsigned nthreads;  // nsite * LsE / spt
-  int kind;           // 0: F32/F32, 1: F16/F16-gauge, 2: F16/BF16-gauge
+  unsigned nthreads;      // nsite * LsE / spt
+  unsigned tile_threads;  // nsite * TE / spt (threads of one tile)
+  int kind;               // 0: F32/F32, 1: F16/F16-gauge, 2: F16/BF16-gauge
   int spt;
+  int TE;                 // slices per tile
+  int lsp;                // compile-time row stride path: 8, 12, 16 or 0 (runtime)
 };
 
-template <int PIN, int GP, int DAG, int N>
-__device__ __forceinline__ void batch_thread(const DhopParams& p, unsigned tid) {
-  const unsigned G = unsigned(p.LsE) / N;
-  const unsigned site = tid / G;
-  const int s0 = int(tid - site * G) * N;
+// One thread of an instance: tile, site and first slice from the thread index.
+template <int PIN, int GP, int DAG, int N, int LSPC>
+__device__ __forceinline__ void batch_thread(const BatchInst& I, unsigned tid) {
+  DhopParams p = I.p;
+  if constexpr (LSPC > 0) {
+    p.LsE = LSPC;
+    p.LsP = LSPC;
+  }
+  const unsigned tile = tid / I.tile_threads;
+  const unsigned r = tid - tile * I.tile_threads;
+  const unsigned G = unsigned(I.TE) / N;
+  const unsigned site = r / G;
+  const int s0 = int(tile) * I.TE + int(r - site * G) * N;
   using T = typename Arith<PIN>::T;
   cpx<T> acc[N][12];
   dhop_thread<PIN, GP, DAG, N>(p, site, s0, acc);
   store_spinor<PIN, N>(p.out, p.out_norm, site, s0, p.LsE, p.LsP, acc);
 }
 
-template <int DAG>
-__global__ void __launch_bounds__(256) k_batch(const BatchInst* __restrict__ inst, int ninst, unsigned total,
-                                               unsigned* next) {
-  __shared__ unsigned item;
-  __shared__ int which;
-  for (;;) {
-    if (threadIdx.x == 0) {
-      item = atomicAdd(next, 1u);
-      // instances are few: find the owner with a binary search over item_begin
-      int lo = 0, hi = ninst - 1;
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (inst[mid].item_begin <= item) lo = mid;
-        else hi = mid - 1;
-      }
-      which = lo;
-    }
-    __syncthreads();
-    const unsigned it = item;
-    const int k = which;
-    __syncthreads();
+template <int PIN, int GP, int DAG, int N>
+__device__ __forceinline__ void batch_by_rows(const BatchInst& I, unsigned tid) {
+  switch (I.lsp) {
+    case 8: batch_thread<PIN, GP, DAG, N, 8>(I, tid); break;
+    case 12: batch_thread<PIN, GP, DAG, N, 12>(I, tid); break;
+    case 16: batch_thread<PIN, GP, DAG, N, 16>(I, tid); break;
+    default: batch_thread<PIN, GP, DAG, N, 0>(I, tid); break;
+  }
+}
+
+template <int PIN, int GP, int DAG>
+__device__ __forceinline__ void batch_by_spt(const BatchInst& I, unsigned tid) {
+  if (I.spt == 2) batch_by_rows<PIN, GP, DAG, 2>(I, tid);
+  else batch_thread<PIN, GP, DAG, 1, 0>(I, tid);
+}
+
+template <int DAG, int T, int MINB>
+__global__ void __launch_bounds__(T, MINB) k_batch(const BatchInst* __restrict__ inst,
+                                                   const unsigned short* __restrict__ item_inst,
+                                                   const unsigned* __restrict__ item_begin, unsigned total,
+                                                   unsigned* next) {
+  // two claimed items: the one being worked on and the next one
+  __shared__ unsigned s_item[2];
+  if (threadIdx.x == 0) {
+    s_item[0] = atomicAdd(next, 1u);
+    s_item[1] = atomicAdd(next, 1u);
+  }
+  __syncthreads();
+  for (int slot = 0;; slot ^= 1) {
+    // the other slot holds a later claim, so once this one is past the end both are
+    const unsigned it = s_item[slot];
     if (it >= total) break;
+    const int k = item_inst[it];
     const BatchInst& I = inst[k];
-    const unsigned tid = (it - I.item_begin) * blockDim.x + threadIdx.x;
+    const unsigned tid = (it - item_begin[k]) * T + threadIdx.x;
     if (tid < I.nthreads) {
-      const DhopParams& p = I.p;
-      if (I.kind == 0) {
-        if (I.spt == 2) batch_thread<GBDW_F32, GBDW_F32, DAG, 2>(p, tid);
-        else batch_thread<GBDW_F32, GBDW_F32, DAG, 1>(p, tid);
-      } else if (I.kind == 1) {
-        if (I.spt == 2) batch_thread<GBDW_F16, GBDW_F16, DAG, 2>(p, tid);
-        else batch_thread<GBDW_F16, GBDW_F16, DAG, 1>(p, tid);
-      } else {
-        if (I.spt == 2) batch_thread<GBDW_F16, GBDW_BF16, DAG, 2>(p, tid);
-        else batch_thread<GBDW_F16, GBDW_BF16, DAG, 1>(p, tid);
-      }
+      if (I.kind == 0) batch_by_spt<GBDW_F32, GBDW_F32, DAG>(I, tid);
+      else if (I.kind == 1) batch_by_spt<GBDW_F16, GBDW_F16, DAG>(I, tid);
+      else batch_by_spt<GBDW_F16, GBDW_BF16, DAG>(I, tid);
     }
+    __syncthreads();  // every thread has read s_item[slot]
+    if (threadIdx.x == 0) s_item[slot] = atomicAdd(next, 1u);
+    __syncthreads();
   }
 }
 
@@ -89,8 +119,12 @@ struct gbdw_batch {
   int dag = 0;
   int threads = 128;
   int spt32 = 2, spt16 = 2;
+  int split = 1;
   BatchInst* d_inst = nullptr;
   unsigned* d_next = nullptr;
+  unsigned* d_begin = nullptr;
+  unsigned short* d_item_inst = nullptr;
+  size_t item_cap = 0;
   unsigned total = 0;
   int grid = 0;
   cudaGraph_t graph = nullptr;
@@ -113,11 +147,46 @@ void release_graph(gbdw_batch* b) {
   b->graph = nullptr;
 }
 
+template <int DAG, int T, int MINB>
+cudaError_t occupancy_of(int* per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_batch<DAG, T, MINB>, T, 0);
+}
+
+template <int DAG>
+cudaError_t occupancy(int threads, int* per_sm) {
+  if (threads == 64) return occupancy_of<DAG, 64, 6>(per_sm);
+  if (threads == 128) return occupancy_of<DAG, 128, 3>(per_sm);
+  return occupancy_of<DAG, 256, 1>(per_sm);
+}
+
+template <int DAG>
+void launch(const gbdw_batch* b, cudaStream_t s) {
+  if (b->threads == 64)
+    k_batch<DAG, 64, 6><<<b->grid, 64, 0, s>>>(b->d_inst, b->d_item_inst, b->d_begin, b->total, b->d_next);
+  else if (b->threads == 128)
+    k_batch<DAG, 128, 3><<<b->grid, 128, 0, s>>>(b->d_inst, b->d_item_inst, b->d_begin, b->total, b->d_next);
+  else
+    k_batch<DAG, 256, 1><<<b->grid, 256, 0, s>>>(b->d_inst, b->d_item_inst, b->d_begin, b->total, b->d_next);
+}
+
+// Tile of an instance for the batch's split: the largest split <= the batch's that cuts the
+// extent into whole slice groups and whose tile is whole values of s (a multiple of nrhs) or
+// whole sets of right-hand sides at one s (a divisor of nrhs).
+int tile_of(int LsE, int nrhs, int spt, int split) {
+  for (int sp = split; sp > 1; sp >>= 1) {
+    if (LsE % sp) continue;
+    const int TE = LsE / sp;
+    if (TE % spt == 0 && (TE % nrhs == 0 || nrhs % TE == 0)) return TE;
+  }
+  return LsE;
+}
+
 // Builds the work list for the current shape and captures [reset counter, persistent kernel].
 int build(gbdw_batch* b) {
   release_graph(b);
   const int n = int(b->g.size());
   std::vector<BatchInst> hi(n);
+  std::vector<unsigned> begin(n);
   // largest instances first so the tail of the dynamic schedule is made of small items
   std::vector<int> order(n);
   for (int i = 0; i < n; ++i) order[i] = i;
@@ -125,6 +194,7 @@ int build(gbdw_batch* b) {
     return b->in[a]->lat->nsite * b->in[a]->LsE > b->in[c]->lat->nsite * b->in[c]->LsE;
   });
   unsigned items = 0;
+  std::vector<unsigned short> item_inst;
   for (int k = 0; k < n; ++k) {
     const int i = order[k];
     BatchInst& I = hi[k];
@@ -135,7 +205,10 @@ int build(gbdw_batch* b) {
     int spt = (I.kind == 0) ? b->spt32 : b->spt16;
     if (x->LsE % spt != 0) spt = 1;
     I.spt = spt;
+    I.TE = tile_of(x->LsE, x->nrhs, spt, b->split);
+    I.lsp = (spt == 2 && x->LsE == x->LsP && (x->LsE == 8 || x->LsE == 12 || x->LsE == 16)) ? x->LsE : 0;
     DhopParams& p = I.p;
+    p = DhopParams{};
     p.U = g->d;
     p.in = x->d;
     p.in_norm = x->norm;
@@ -153,25 +226,36 @@ int build(gbdw_batch* b) {
     p.result = nullptr;
     p.err = nullptr;
     I.nthreads = unsigned(p.nsite * (p.LsE / spt));
-    I.item_begin = items;
-    items += (I.nthreads + b->threads - 1) / b->threads;
+    I.tile_threads = unsigned(p.nsite * (I.TE / spt));
+    begin[k] = items;
+    const unsigned nit = (I.nthreads + b->threads - 1) / b->threads;
+    item_inst.insert(item_inst.end(), nit, (unsigned short)k);
+    items += nit;
   }
   b->total = items;
+  if (item_inst.size() > b->item_cap) {
+    if (b->d_item_inst) cudaFree(b->d_item_inst);
+    b->d_item_inst = nullptr;
+    b->item_cap = 0;
+    GBDW_CUDA(dev_alloc((void**)&b->d_item_inst, item_inst.size() * sizeof(unsigned short)));
+    b->item_cap = item_inst.size();
+  }
   GBDW_CUDA(cudaMemcpyAsync(b->d_inst, hi.data(), sizeof(BatchInst) * n, cudaMemcpyHostToDevice, stream()));
+  GBDW_CUDA(cudaMemcpyAsync(b->d_begin, begin.data(), sizeof(unsigned) * n, cudaMemcpyHostToDevice, stream()));
+  GBDW_CUDA(cudaMemcpyAsync(b->d_item_inst, item_inst.data(), item_inst.size() * sizeof(unsigned short),
+                            cudaMemcpyHostToDevice, stream()));
   int per_sm = 0;
-  if (b->dag)
-    GBDW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<1>, b->threads, 0));
-  else
-    GBDW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<0>, b->threads, 0));
+  GBDW_CUDA(b->dag ? occupancy<1>(b->threads, &per_sm) : occupancy<0>(b->threads, &per_sm));
   if (per_sm < 1) per_sm = 1;
   b->grid = num_sms() * per_sm;
   if (unsigned(b->grid) > items) b->grid = int(items);
+  // the host vectors above must outlive the queued copies
   GBDW_CUDA(cudaStreamSynchronize(stream()));
   cudaStream_t s = stream();
   GBDW_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   cudaMemsetAsync(b->d_next, 0, sizeof(unsigned), s);
-  if (b->dag) k_batch<1><<<b->grid, b->threads, 0, s>>>(b->d_inst, n, b->total, b->d_next);
-  else k_batch<0><<<b->grid, b->threads, 0, s>>>(b->d_inst, n, b->total, b->d_next);
+  if (b->dag) launch<1>(b, s);
+  else launch<0>(b, s);
   cudaError_t le = cudaGetLastError();
   cudaError_t ce = cudaStreamEndCapture(s, &b->graph);
   if (le != cudaSuccess) return cuda_fail(le, "k_batch capture");
@@ -189,39 +273,48 @@ int replay(gbdw_batch* b) {
 // Times graph replays for each admissible shape and keeps the fastest.
 int tune(gbdw_batch* b) {
   bool any16 = false, any32 = false;
-  for (size_t i = 0; i < b->in.size(); ++i) (b->in[i]->prec == GBDW_F16 ? any16 : any32) = true;
+  int max_split = 1;
+  for (size_t i = 0; i < b->in.size(); ++i) {
+    (b->in[i]->prec == GBDW_F16 ? any16 : any32) = true;
+    max_split = std::max(max_split, b->in[i]->LsE / 2);
+  }
   const int threads_c[] = {64, 128, 256};
-  const int spt_c[] = {1, 2};
+  const int spt_c[] = {2, 1};
+  const int split_c[] = {1, 2, 4, 8};
   cudaEvent_t e0, e1;
   GBDW_CUDA(cudaEventCreate(&e0));
   GBDW_CUDA(cudaEventCreate(&e1));
   float best = 1e30f;
-  int bt = b->threads, b32 = b->spt32, b16 = b->spt16;
+  int bt = b->threads, b32 = b->spt32, b16 = b->spt16, bsp = b->split;
   int st = GBDW_OK;
   for (int th : threads_c)
     for (int s32 : spt_c)
-      for (int s16 : spt_c) {
-        if (!any32 && s32 != spt_c[0]) continue;
-        if (!any16 && s16 != spt_c[0]) continue;
-        b->threads = th;
-        b->spt32 = s32;
-        b->spt16 = s16;
-        if ((st = build(b))) goto done;
-        if ((st = replay(b))) goto done;
-        cudaEventRecord(e0, stream());
-        for (int r = 0; r < 3; ++r)
+      for (int s16 : spt_c)
+        for (int sp : split_c) {
+          if (!any32 && s32 != spt_c[0]) continue;
+          if (!any16 && s16 != spt_c[0]) continue;
+          if (sp > max_split) continue;
+          b->threads = th;
+          b->spt32 = s32;
+          b->spt16 = s16;
+          b->split = sp;
+          if ((st = build(b))) goto done;
           if ((st = replay(b))) goto done;
-        cudaEventRecord(e1, stream());
-        cudaEventSynchronize(e1);
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < best) {
-          best = ms;
-          bt = th;
-          b32 = s32;
-          b16 = s16;
+          cudaEventRecord(e0, stream());
+          for (int r = 0; r < 3; ++r)
+            if ((st = replay(b))) goto done;
+          cudaEventRecord(e1, stream());
+          cudaEventSynchronize(e1);
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, e0, e1);
+          if (ms < best) {
+            best = ms;
+            bt = th;
+            b32 = s32;
+            b16 = s16;
+            bsp = sp;
+          }
         }
-      }
 done:
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -229,6 +322,7 @@ done:
   b->threads = bt;
   b->spt32 = b32;
   b->spt16 = b16;
+  b->split = bsp;
   return build(b);
 }
 
@@ -238,8 +332,8 @@ extern "C" {
 
 int gbdw_batch_create(gbdw_batch** out, int n, const gbdw_gauge* const* gauges, gbdw_field* const* outs,
                       const gbdw_field* const* ins, int dag) {
-  if (!out || n < 1 || !gauges || !outs || !ins) {
-    set_error("gbdw_batch_create: invalid arguments");
+  if (!out || n < 1 || n > 65535 || !gauges || !outs || !ins) {
+    set_error("gbdw_batch_create: invalid arguments (1 to 65535 instances)");
     return GBDW_ERR_INVALID;
   }
   for (int i = 0; i < n; ++i) {
@@ -264,10 +358,10 @@ int gbdw_batch_create(gbdw_batch** out, int n, const gbdw_gauge* const* gauges, 
   b->in.assign(ins, ins + n);
   b->dag = dag ? 1 : 0;
   cudaError_t e = dev_alloc((void**)&b->d_inst, sizeof(BatchInst) * n);
+  if (e == cudaSuccess) e = dev_alloc((void**)&b->d_begin, sizeof(unsigned) * n);
   if (e == cudaSuccess) e = dev_alloc((void**)&b->d_next, 64);
   if (e != cudaSuccess) {
-    if (b->d_inst) cudaFree(b->d_inst);
-    delete b;
+    gbdw_batch_destroy(b);
     return cuda_fail(e, "cudaMalloc(batch)");
   }
   if (int st = tune(b)) {
@@ -288,6 +382,8 @@ int gbdw_batch_destroy(gbdw_batch* b) {
   cudaStreamSynchronize(stream());
   release_graph(b);
   if (b->d_inst) cudaFree(b->d_inst);
+  if (b->d_begin) cudaFree(b->d_begin);
+  if (b->d_item_inst) cudaFree(b->d_item_inst);
   if (b->d_next) cudaFree(b->d_next);
   delete b;
   return GBDW_OK;
@@ -299,6 +395,28 @@ int gbdw_batch_info(const gbdw_batch* b, int64_t info[4]) {
   info[1] = b->grid;
   info[2] = b->threads;
   info[3] = b->exec ? 1 : 0;
+  return GBDW_OK;
+}
+
+int gbdw_batch_set_shape(gbdw_batch* b, const int shape[4]) {
+  if (!b || !shape || (shape[0] != 64 && shape[0] != 128 && shape[0] != 256) || shape[1] < 1 || shape[1] > 2 ||
+      shape[2] < 1 || shape[2] > 2 || shape[3] < 1 || (shape[3] & (shape[3] - 1))) {
+    set_error("gbdw_batch_set_shape: threads 64/128/256, slices per thread 1 or 2, split a power of two");
+    return GBDW_ERR_INVALID;
+  }
+  b->threads = shape[0];
+  b->spt32 = shape[1];
+  b->spt16 = shape[2];
+  b->split = shape[3];
+  return build(b);
+}
+
+int gbdw_batch_shape(const gbdw_batch* b, int shape[4]) {
+  if (!b || !shape) return GBDW_ERR_INVALID;
+  shape[0] = b->threads;
+  shape[1] = b->spt32;
+  shape[2] = b->spt16;
+  shape[3] = b->split;
   return GBDW_OK;
 }
 

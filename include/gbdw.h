@@ -323,8 +323,9 @@ int gbdw_static_data_write(const char* h_path, const char* cc_path, uint64_t nsi
                            const uint64_t* nbr, const uint8_t* prm);
 
 /* ------------------------------------------------------------------ batched persistent Dhop
- * Many independent instances (own lattice, gauge field, Ls and precision) in one persistent
- * launch, replayed through a CUDA graph. */
+ * Many independent instances (own lattice, gauge field, Ls, right-hand sides and precision) in
+ * one persistent launch, replayed through a CUDA graph; the launch shape and the Ls / RHS
+ * tiling are chosen by timing the caller's own batch at creation. */
 typedef struct gbdw_batch gbdw_batch;
 int gbdw_batch_create(gbdw_batch** b, int n, const gbdw_gauge* const* gauges,
                       gbdw_field* const* outs, const gbdw_field* const* ins, int dag);
@@ -332,6 +333,14 @@ int gbdw_batch_run(gbdw_batch* b);        /* one graph replay */
 int gbdw_batch_destroy(gbdw_batch* b);
 /* info[0]=work items info[1]=persistent CTAs info[2]=threads per CTA info[3]=graph (1/0) */
 int gbdw_batch_info(const gbdw_batch* b, int64_t info[4]);
+/* The autotuned shape: shape[0] threads per CTA, shape[1] / shape[2] slices per thread of the
+ * FP32 / FP16 instances, shape[3] tile split (each site's Ls*nrhs slices are cut into up to
+ * this many contiguous tiles: an Ls tile of some values of s with every right-hand side, or an
+ * RHS tile of some right-hand sides at one s). */
+int gbdw_batch_shape(const gbdw_batch* b, int shape[4]);
+/* Pins a shape (same meaning; threads 64/128/256, slices per thread 1 or 2, split a power of two)
+ * and rebuilds the graph. */
+int gbdw_batch_set_shape(gbdw_batch* b, const int shape[4]);
 
 /* ------------------------------------------------------------------ autotuner
  * Times the launch shapes of the hopping kernel for (g, field) and stores the fastest in
