@@ -6,19 +6,20 @@
 // of one site; the slices of a site are cut into `split` contiguous tiles of TE = LsE/split
 // slices, so a tile holds TE/nrhs values of s with all right-hand sides (an Ls tile) or, when
 // TE < nrhs, TE of the right-hand sides at one s (an RHS tile).  Threads are ordered (tile,
-// site, slice group), and an instance's threads are cut into work items of one CTA each.  The
+// site, slice group), and an instance's threads are cut into work items of one warp each.  The
 // link of a (site, leg) is loaded once per thread group and reused over its tile's slices;
 // more tiles put more sites in a CTA.
 //
-// Scheduling.  A grid of (SMs x resident CTAs per SM) CTAs pulls items from a device counter;
-// each CTA claims its next item while it works on the current one, so the atomic's latency is
-// hidden and uneven volumes still balance dynamically.  Items run largest instance first.
+// Scheduling.  A grid of (SMs x resident CTAs per SM) CTAs pulls items from a device counter,
+// warp by warp; each warp claims its next item while it works on the current one, so the
+// atomic's latency is hidden and uneven volumes still balance dynamically.  Items run largest
+// instance first.
 // The loop is bounded by the item count and never waits on another CTA.  A memset node in the
 // same graph resets the counter.
 //
-// Kernels.  Rows of 8, 12 or 16 slots (Ls = 8/12/16 with one right-hand side) take a path with
-// the row stride a compile-time constant, as the single-instance specialised form does; other
-// extents take the runtime-stride path.  Registers are capped so that (threads x CTAs per SM)
+// Kernels.  Rows of 8, 12, 16, 24, 32, 48 or 64 slots (Ls = 8/12/16 with 1, 2 or 4 right-hand
+// sides) take a path with the row stride a compile-time constant, as the single-instance
+// specialised form does; other extents, and BF16 links, take the runtime-stride path.  Registers are capped so that (threads x CTAs per SM)
 // ~ 384 threads stay resident, the operating point of the single-instance kernels.
 //
 // Tuning.  The shape (threads per CTA, slices per thread for FP32 and FP16 instances, tile
@@ -63,11 +64,19 @@ __device__ __forceinline__ void batch_thread(const BatchInst& I, unsigned tid) {
 
 template <int PIN, int GP, int DAG, int N>
 __device__ __forceinline__ void batch_by_rows(const BatchInst& I, unsigned tid) {
-  switch (I.lsp) {
-    case 8: batch_thread<PIN, GP, DAG, N, 8>(I, tid); break;
-    case 12: batch_thread<PIN, GP, DAG, N, 12>(I, tid); break;
-    case 16: batch_thread<PIN, GP, DAG, N, 16>(I, tid); break;
-    default: batch_thread<PIN, GP, DAG, N, 0>(I, tid); break;
+  if constexpr (GP == GBDW_BF16) {
+    batch_thread<PIN, GP, DAG, N, 0>(I, tid);
+  } else {
+    switch (I.lsp) {
+      case 8: batch_thread<PIN, GP, DAG, N, 8>(I, tid); break;
+      case 12: batch_thread<PIN, GP, DAG, N, 12>(I, tid); break;
+      case 16: batch_thread<PIN, GP, DAG, N, 16>(I, tid); break;
+      case 24: batch_thread<PIN, GP, DAG, N, 24>(I, tid); break;
+      case 32: batch_thread<PIN, GP, DAG, N, 32>(I, tid); break;
+      case 48: batch_thread<PIN, GP, DAG, N, 48>(I, tid); break;
+      case 64: batch_thread<PIN, GP, DAG, N, 64>(I, tid); break;
+      default: batch_thread<PIN, GP, DAG, N, 0>(I, tid); break;
+    }
   }
 }
 
@@ -77,33 +86,36 @@ __device__ __forceinline__ void batch_by_spt(const BatchInst& I, unsigned tid) {
   else batch_thread<PIN, GP, DAG, 1, 0>(I, tid);
 }
 
+// Work items are one warp each; every warp claims its own items (lane 0 takes the next one
+// from the counter while the warp works on the current one), so the warps of a CTA never wait
+// for each other.
 template <int DAG, int T, int MINB>
 __global__ void __launch_bounds__(T, MINB) k_batch(const BatchInst* __restrict__ inst,
                                                    const unsigned short* __restrict__ item_inst,
                                                    const unsigned* __restrict__ item_begin, unsigned total,
                                                    unsigned* next) {
-  // two claimed items: the one being worked on and the next one
-  __shared__ unsigned s_item[2];
-  if (threadIdx.x == 0) {
-    s_item[0] = atomicAdd(next, 1u);
-    s_item[1] = atomicAdd(next, 1u);
+  const unsigned lane = threadIdx.x & 31u;
+  unsigned cur = 0, nxt = 0;
+  if (lane == 0) {
+    cur = atomicAdd(next, 1u);
+    nxt = atomicAdd(next, 1u);
   }
-  __syncthreads();
-  for (int slot = 0;; slot ^= 1) {
-    // the other slot holds a later claim, so once this one is past the end both are
-    const unsigned it = s_item[slot];
-    if (it >= total) break;
-    const int k = item_inst[it];
+  cur = __shfl_sync(0xffffffffu, cur, 0);
+  nxt = __shfl_sync(0xffffffffu, nxt, 0);
+  // claims only grow, so once the current item is past the end the queued one is too
+  while (cur < total) {
+    unsigned claim = 0;
+    if (lane == 0) claim = atomicAdd(next, 1u);  // latency hidden behind the work below
+    const int k = item_inst[cur];
     const BatchInst& I = inst[k];
-    const unsigned tid = (it - item_begin[k]) * T + threadIdx.x;
+    const unsigned tid = (cur - item_begin[k]) * 32u + lane;
     if (tid < I.nthreads) {
       if (I.kind == 0) batch_by_spt<GBDW_F32, GBDW_F32, DAG>(I, tid);
       else if (I.kind == 1) batch_by_spt<GBDW_F16, GBDW_F16, DAG>(I, tid);
       else batch_by_spt<GBDW_F16, GBDW_BF16, DAG>(I, tid);
     }
-    __syncthreads();  // every thread has read s_item[slot]
-    if (threadIdx.x == 0) s_item[slot] = atomicAdd(next, 1u);
-    __syncthreads();
+    cur = nxt;
+    nxt = __shfl_sync(0xffffffffu, claim, 0);
   }
 }
 
@@ -155,18 +167,15 @@ cudaError_t occupancy_of(int* per_sm) {
 template <int DAG>
 cudaError_t occupancy(int threads, int* per_sm) {
   if (threads == 64) return occupancy_of<DAG, 64, 6>(per_sm);
-  if (threads == 128) return occupancy_of<DAG, 128, 3>(per_sm);
-  return occupancy_of<DAG, 256, 1>(per_sm);
+  return occupancy_of<DAG, 128, 3>(per_sm);
 }
 
 template <int DAG>
 void launch(const gbdw_batch* b, cudaStream_t s) {
   if (b->threads == 64)
     k_batch<DAG, 64, 6><<<b->grid, 64, 0, s>>>(b->d_inst, b->d_item_inst, b->d_begin, b->total, b->d_next);
-  else if (b->threads == 128)
-    k_batch<DAG, 128, 3><<<b->grid, 128, 0, s>>>(b->d_inst, b->d_item_inst, b->d_begin, b->total, b->d_next);
   else
-    k_batch<DAG, 256, 1><<<b->grid, 256, 0, s>>>(b->d_inst, b->d_item_inst, b->d_begin, b->total, b->d_next);
+    k_batch<DAG, 128, 3><<<b->grid, 128, 0, s>>>(b->d_inst, b->d_item_inst, b->d_begin, b->total, b->d_next);
 }
 
 // Tile of an instance for the batch's split: the largest split <= the batch's that cuts the
@@ -206,7 +215,9 @@ int build(gbdw_batch* b) {
     if (x->LsE % spt != 0) spt = 1;
     I.spt = spt;
     I.TE = tile_of(x->LsE, x->nrhs, spt, b->split);
-    I.lsp = (spt == 2 && x->LsE == x->LsP && (x->LsE == 8 || x->LsE == 12 || x->LsE == 16)) ? x->LsE : 0;
+    const int L = x->LsE;
+    I.lsp = (spt == 2 && L == x->LsP &&
+             (L == 8 || L == 12 || L == 16 || L == 24 || L == 32 || L == 48 || L == 64)) ? L : 0;
     DhopParams& p = I.p;
     p = DhopParams{};
     p.U = g->d;
@@ -228,7 +239,7 @@ int build(gbdw_batch* b) {
     I.nthreads = unsigned(p.nsite * (p.LsE / spt));
     I.tile_threads = unsigned(p.nsite * (I.TE / spt));
     begin[k] = items;
-    const unsigned nit = (I.nthreads + b->threads - 1) / b->threads;
+    const unsigned nit = (I.nthreads + 31) / 32;
     item_inst.insert(item_inst.end(), nit, (unsigned short)k);
     items += nit;
   }
@@ -278,7 +289,7 @@ int tune(gbdw_batch* b) {
     (b->in[i]->prec == GBDW_F16 ? any16 : any32) = true;
     max_split = std::max(max_split, b->in[i]->LsE / 2);
   }
-  const int threads_c[] = {64, 128, 256};
+  const int threads_c[] = {64, 128};
   const int spt_c[] = {2, 1};
   const int split_c[] = {1, 2, 4, 8};
   cudaEvent_t e0, e1;
@@ -399,9 +410,9 @@ int gbdw_batch_info(const gbdw_batch* b, int64_t info[4]) {
 }
 
 int gbdw_batch_set_shape(gbdw_batch* b, const int shape[4]) {
-  if (!b || !shape || (shape[0] != 64 && shape[0] != 128 && shape[0] != 256) || shape[1] < 1 || shape[1] > 2 ||
+  if (!b || !shape || (shape[0] != 64 && shape[0] != 128) || shape[1] < 1 || shape[1] > 2 ||
       shape[2] < 1 || shape[2] > 2 || shape[3] < 1 || (shape[3] & (shape[3] - 1))) {
-    set_error("gbdw_batch_set_shape: threads 64/128/256, slices per thread 1 or 2, split a power of two");
+    set_error("gbdw_batch_set_shape: threads 64/128, slices per thread 1 or 2, split a power of two");
     return GBDW_ERR_INVALID;
   }
   b->threads = shape[0];

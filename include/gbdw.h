@@ -338,7 +338,7 @@ int gbdw_batch_info(const gbdw_batch* b, int64_t info[4]);
  * this many contiguous tiles: an Ls tile of some values of s with every right-hand side, or an
  * RHS tile of some right-hand sides at one s). */
 int gbdw_batch_shape(const gbdw_batch* b, int shape[4]);
-/* Pins a shape (same meaning; threads 64/128/256, slices per thread 1 or 2, split a power of two)
+/* Pins a shape (same meaning; threads 64/128, slices per thread 1 or 2, split a power of two)
  * and rebuilds the graph. */
 int gbdw_batch_set_shape(gbdw_batch* b, const int shape[4]);
 
