@@ -836,13 +836,18 @@ def run_only(args) -> dict:
             "shape": list(gb.tune_query(g, xs[0])), "gpu_launches": int(launches)}
 
 
-AUX_ONLY = ("mobius_m", "halo_pack")
+AUX_ONLY = ("mobius_m", "halo_pack", "batch", "batch_rhs")
 
 
 def run_aux_only(args) -> dict:
     """The Mobius operator (b = 1.5, c = 0.5, M5 = 1.8, mf = 0.01) or the one-launch pack of all
-    eight halo faces, FP32 16^4 x 16, nothing else (for profiling)."""
+    eight halo faces, FP32 16^4 x 16, or one of the 64-instance batches, nothing else (for
+    profiling)."""
     import gridbench_gb300 as gb
+    if args.only.startswith("batch"):
+        peak, _ = measured_peak_hbm()
+        return {"workload": args.only, **(bench_batch(gb, peak) if args.only == "batch" else
+                                          bench_batch(gb, peak, (1, 2, 4), seed=2025))}
     lat = gb.Lattice.periodic(DIMS, LS)
     g = gb.Gauge(lat, None, gb.F32, seed=11)
     xs = [gb.Field(lat, gb.F32).gaussian(21 + i) for i in range(4)]
