@@ -622,7 +622,10 @@ __device__ __forceinline__ void dhop_thread(const DhopParams& p, unsigned site, 
     LinkIO<GP>::load(p.U, size_t(site) * 8 + L, u);                                                    \
     hop_leg<PIN, DAG, N, L, false>(u, p.in, n * 12, s0, p.LsP, p.in_norm + n * p.LsE + s0, acc);       \
   }
-  GBDW_LEG(0) GBDW_LEG(1) GBDW_LEG(2) GBDW_LEG(3) GBDW_LEG(4) GBDW_LEG(5) GBDW_LEG(6) GBDW_LEG(7)
+  // each forward leg next to its backward partner: the x-neighbours of a CTA's sites are the
+  // CTA's own sites, and a spinor one thread reads for X+ is read again for X- by the thread
+  // of the site two steps along x while its lines are still in L1
+  GBDW_LEG(0) GBDW_LEG(4) GBDW_LEG(1) GBDW_LEG(5) GBDW_LEG(2) GBDW_LEG(6) GBDW_LEG(3) GBDW_LEG(7)
 #undef GBDW_LEG
   acc.unpack(out);
 }
