@@ -575,9 +575,6 @@ def bench_cg(gb, args) -> dict:
                                                                    g32=g32)),
         ("full_mixed_fp16", 0.03, lambda x, d: gb.cg_solve(g64, x, b, M5, mf, gb.CG_MIXED, max_iter=it, delta=d, g32=g32,
                                                           gsloppy=g16, sloppy_prec=gb.F16, sloppy_residual=1)),
-        ("full_mixed_fp16_x16", 0.03, lambda x, d: gb.cg_solve(g64, x, b, M5, mf, gb.CG_MIXED, max_iter=it, delta=d,
-                                                              g32=g32, gsloppy=g16, sloppy_prec=gb.F16,
-                                                              sloppy_residual=2)),
         ("full_mixed_fp32", 1e-4, lambda x, d: gb.cg_solve(g64, x, b, M5, mf, gb.CG_MIXED, max_iter=it, delta=d,
                                                            g32=g32, gsloppy=g32, sloppy_prec=gb.F32)),
         ("eo_plain_fp32_fp64res", 1e-4, lambda x, d: gb.cg_solve_eo(G64, x, b, M5, mf, gb.CG_PLAIN, max_iter=it,
@@ -585,9 +582,6 @@ def bench_cg(gb, args) -> dict:
         ("eo_mixed_fp16", 0.02, lambda x, d: gb.cg_solve_eo(G64, x, b, M5, mf, gb.CG_MIXED, max_iter=it, delta=d,
                                                             g32=G32, gsloppy=G16, sloppy_prec=gb.F16,
                                                             sloppy_residual=1)),
-        ("eo_mixed_fp16_x16", 0.02, lambda x, d: gb.cg_solve_eo(G64, x, b, M5, mf, gb.CG_MIXED, max_iter=it,
-                                                                delta=d, g32=G32, gsloppy=G16, sloppy_prec=gb.F16,
-                                                                sloppy_residual=2)),
         ("eo_mixed_fp32", 1e-4, lambda x, d: gb.cg_solve_eo(G64, x, b, M5, mf, gb.CG_MIXED, max_iter=it, delta=d,
                                                             g32=G32, gsloppy=G32, sloppy_prec=gb.F32)),
     )
@@ -603,7 +597,7 @@ def bench_cg(gb, args) -> dict:
         del x
     for pre in ("full", "eo"):
         plain = res.get(f"{pre}_plain_fp32_fp64res", {})
-        for sp in ("fp16", "fp16_x16", "fp32"):
+        for sp in ("fp16", "fp32"):
             mixed = res.get(f"{pre}_mixed_{sp}", {})
             if "seconds" in plain and "seconds" in mixed:
                 res[f"speedup_{pre}_mixed_{sp}_vs_plain"] = round(plain["seconds"] / mixed["seconds"], 3)

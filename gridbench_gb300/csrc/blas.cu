@@ -390,16 +390,6 @@ int blas_cg_r(double alpha, gbdw_field* r, const gbdw_field* ap, double* rr) {
 int blas_cg_xp(double alpha, double beta, gbdw_field* x, gbdw_field* p, const gbdw_field* r, gbdw_field* q) {
   const int64_t ns = r->lat->nsite;
   const int L = r->LsE;
-  if (!q && pairs_ok(x) && pairs_ok(p) && pairs_ok(r) && x->prec == GBDW_F16) {
-    if (p->prec != GBDW_F16 || r->prec != GBDW_F16) {
-      set_error("blas_cg_xp: an FP16 iterated solution needs FP16 p and r");
-      return GBDW_ERR_INVALID;
-    }
-    const unsigned g = unsigned(grid_pairs(r));
-    k_cg_xp_pairs<GBDW_F16, GBDW_F16, GBDW_F16><<<g, kThreads, 0, stream()>>>(alpha, beta, out(x), out(p), ref(r), ns, L);
-    GBDW_LAUNCHED();
-    return GBDW_OK;
-  }
   if (!q && pairs_ok(x) && pairs_ok(p) && pairs_ok(r) && x->prec == GBDW_F32) {
     const unsigned g = unsigned(grid_pairs(r));
     if (p->prec == GBDW_F16 && r->prec == GBDW_F16)
@@ -429,7 +419,6 @@ int blas_cg_xp(double alpha, double beta, gbdw_field* x, gbdw_field* p, const gb
     GBDW_XP(GBDW_F32, GBDW_F16, GBDW_F32, -1)
     GBDW_XP(GBDW_F32, GBDW_F32, GBDW_F32, -1)
     GBDW_XP(GBDW_F32, GBDW_F16, GBDW_F16, -1)
-    GBDW_XP(GBDW_F16, GBDW_F16, GBDW_F16, -1)
     default:
       set_error("blas_cg_xp: unsupported precision combination");
       return GBDW_ERR_INVALID;

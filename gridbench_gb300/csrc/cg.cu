@@ -81,13 +81,10 @@ int cg_core(const Problem& P, int mode, gbdw_field* x, const gbdw_field* b, cons
     TRY(F.make(lat, GBDW_F32, &ap));
   } else {
     // the iterated residual: FP32, or FP16 on request when the whole sloppy operator is FP16
-    const bool half = (prm->sloppy_residual == 1 || prm->sloppy_residual == 2) && P.op_prec == GBDW_F16 &&
-                      P.half_residual_ok;
-    const int rprec = half ? GBDW_F16 : GBDW_F32;
-    // the solution's increment since the last reliable update: FP16 (per-slice norms) on request,
-    // which rounds each increment at the sloppy operator's own precision
-    const int xprec = (half && prm->sloppy_residual == 2) ? GBDW_F16 : GBDW_F32;
-    TRY(F.make(lat, xprec, &xs));
+    const int rprec = (prm->sloppy_residual == 1 && P.op_prec == GBDW_F16 && P.half_residual_ok) ? GBDW_F16 : GBDW_F32;
+    // the solution's increment since the last reliable update stays FP32: summing hundreds of
+    // small increments into an FP16 accumulator loses them (measured: no convergence)
+    TRY(F.make(lat, GBDW_F32, &xs));
     TRY(F.make(lat, rprec, &rs));
     TRY(F.make(lat, P.op_prec, &p));
     TRY(F.make(lat, P.op_prec, &ap));

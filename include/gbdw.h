@@ -176,9 +176,7 @@ typedef struct {
   int sloppy_prec;      /* GBDW_F16 or GBDW_F32 for GBDW_CG_MIXED */
   int sloppy_gauge;     /* GBDW_F16, GBDW_BF16 or GBDW_F32 */
   int sloppy_residual;  /* GBDW_CG_MIXED with FP16 spinors and FP16 links: 1 keeps the iterated
-                           residual in FP16 (per-slice norms) instead of FP32; 2 also keeps the
-                           solution's increment since the last reliable update in FP16 (it is
-                           folded into the FP64 solution at every reliable update); 0 otherwise */
+                           residual in FP16 (per-slice norms) instead of FP32; 0 otherwise */
 } gbdw_cg_params;
 typedef struct {
   int iterations;

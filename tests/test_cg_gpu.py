@@ -87,15 +87,13 @@ def test_cg_reliable_update_threshold_extremes(setup, delta):
 
 
 @pytest.mark.parametrize("delta", [0.03, 0.1])
-@pytest.mark.parametrize("sloppy_residual", [1, 2])
-def test_cg_mixed_fp16_residual(setup, delta, sloppy_residual):
+def test_cg_mixed_fp16_residual(setup, delta):
     """The mixed FP16 solve with its iterated residual stored in FP16 (the fused adjoint pass
-    updates r in FP16 with per-slice norms), and with the solution's increment between reliable
-    updates in FP16 as well (sloppy_residual = 2), still reaches the 1e-10 true residual."""
+    updates r in FP16 with per-slice norms) still reaches the 1e-10 true residual."""
     c, lat, g64, g32, g16, b, Ls = setup
     x = gb.Field(lat, gb.F64)
     st = gb.cg_solve(g64, x, b, M5, MF, gb.CG_MIXED, tol=1e-10, max_iter=5000, delta=delta, g32=g32,
-                     gsloppy=g16, sloppy_prec=gb.F16, sloppy_residual=sloppy_residual)
-    print(delta, sloppy_residual, st)
+                     gsloppy=g16, sloppy_prec=gb.F16, sloppy_residual=1)
+    print(delta, st)
     assert st["true_residual"] <= 1e-10
     assert _true_residual(c, x.numpy(), Ls) <= 2e-10

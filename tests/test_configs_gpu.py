@@ -144,7 +144,7 @@ def cg32(gpu):
     return {"U": U, "phi": phi, "nbr": nbr, "nsite": nsite, "Ls": Ls, "lat": lat, "g": gs, "b": b}
 
 
-@pytest.mark.parametrize("mode", ["plain", "mixed_fp16", "mixed_fp16_x16"])
+@pytest.mark.parametrize("mode", ["plain", "mixed_fp16"])
 def test_cg_32x16_true_residual_recomputed_by_oracle(cg32, mode):
     """CG on M^dag M (Shamir, M5 = 1.8, mf = 0.01) at 32^4 x Ls=16 to a 1e-10 true residual,
     plain (FP32 operator, FP64 vectors) and mixed (FP16 operator and iterated residual,
@@ -157,7 +157,7 @@ def test_cg_32x16_true_residual_recomputed_by_oracle(cg32, mode):
         st = gb.cg_solve(g[gb.F64], x, c["b"], 1.8, 0.01, gb.CG_PLAIN, delta=1e-4, g32=g[gb.F32])
     else:
         st = gb.cg_solve(g[gb.F64], x, c["b"], 1.8, 0.01, gb.CG_MIXED, delta=0.03, g32=g[gb.F32],
-                         gsloppy=g[gb.F16], sloppy_prec=gb.F16, sloppy_residual=2 if mode.endswith("x16") else 1)
+                         gsloppy=g[gb.F16], sloppy_prec=gb.F16, sloppy_residual=1)
     assert st["true_residual"] <= 1e-10
     xs = x.numpy()
     del x
