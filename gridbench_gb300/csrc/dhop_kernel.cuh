@@ -64,23 +64,10 @@ __device__ __forceinline__ void store_norms(float* nrm, int64_t e, const float (
   }
 }
 
-// ------------------------------------------------------------------ FP16 -> FP32 on the ALU
-// The two halves of w as floats times 2^-112, exactly: each half's exponent and mantissa bits are
-// moved into a float's (the biases differ by 127 - 15 = 112; subnormal halves land on float
-// subnormals with the same factor, zero stays zero).  Only integer operations: they run on the
-// ALU pipe, which the FP16 hopping kernel leaves mostly idle, instead of the FMA pipe that bounds
-// it.  The factor 2^112 is restored once per leg (on the neighbour's norm) or per link entry.
-constexpr float kHalfRescale = 0x1p112f;
-__device__ __forceinline__ float2 h2f_scaled(unsigned w) {
-  const unsigned lo = ((w & 0x7fffu) << 13) | ((w & 0x8000u) << 16);
-  const unsigned hi = ((w >> 3) & 0x0fffe000u) | (w & 0x80000000u);
-  return make_float2(__uint_as_float(lo), __uint_as_float(hi));
-}
-
 // ------------------------------------------------------------------ links
 // Full 3x3 (F64/F32) or two rows with the third rebuilt as conj(r0 x r1) (exact for SU(3)).
 __device__ __forceinline__ cpx<float> h2c(unsigned w) {
-  const float2 f = __fmul2_rn(h2f_scaled(w), make_float2(kHalfRescale, kHalfRescale));
+  const float2 f = h2f(w);
   return {f.x, f.y};
 }
 __device__ __forceinline__ cpx<float> b2c(unsigned w) {
@@ -226,7 +213,6 @@ __device__ __forceinline__ cp2 su3_row2(const cpx<float> (&u)[3], const cp2 (&h)
 // nrm points at the F16 norms of its first slice.
 // x + c*y on stored FP16 pairs (Re pair in .x, Im pair in .y), c a unit; both operands share
 // the site norm, so the sum is formed before the conversion to FP32.
-// The result is in FP32 times 2^-112 (h2f_scaled); the caller restores the factor on the norm.
 template <int C>
 __device__ __forceinline__ cp2 hproj(uint2 x, uint2 y) {
   const __half2 xr = *reinterpret_cast<__half2*>(&x.x), xi = *reinterpret_cast<__half2*>(&x.y);
@@ -236,7 +222,7 @@ __device__ __forceinline__ cp2 hproj(uint2 x, uint2 y) {
   else if constexpr (C == 1) { r = __hsub2(xr, yr); i = __hsub2(xi, yi); }
   else if constexpr (C == 2) { r = __hsub2(xr, yi); i = __hadd2(xi, yr); }   // + i y
   else { r = __hadd2(xr, yi); i = __hsub2(xi, yr); }                         // - i y
-  return {h2f_scaled(*reinterpret_cast<unsigned*>(&r)), h2f_scaled(*reinterpret_cast<unsigned*>(&i))};
+  return {__half22float2(r), __half22float2(i)};
 }
 
 template <int PIN, int DAG, int NP, int L, bool SMEM>
@@ -275,9 +261,7 @@ __device__ __forceinline__ void hop_leg_pairs(const cpx<float> (&u)[3][3], const
     // accumulated (FFMA2 in place of FADD2) instead of every projected component
 #pragma unroll
     for (int q = 0; q < NP; ++q) {
-      // the projected components carry 2^-112 (hproj): restore it on the norm
-      const float2 nr = __fmul2_rn(ldv<SMEM>(reinterpret_cast<const float2*>(nrm) + q),
-                                   make_float2(kHalfRescale, kHalfRescale));
+      const float2 nr = ldv<SMEM>(reinterpret_cast<const float2*>(nrm) + q);
       const float2 nn = neg2(nr);
 #pragma unroll
       for (int r = 0; r < 3; ++r) {
