@@ -53,6 +53,12 @@ bool blocked_ok(const gbdw_lattice* lat, const gbdw_field* in) {
   return true;
 }
 
+bool mobius_fusable(const gbdw_gauge* g, const gbdw_field* in) {
+  const int Ls = g->lat->Ls;
+  return g->lat->fast && in->prec == GBDW_F32 && in->nrhs == 1 && in->LsE == in->LsP && Ls >= 2 && Ls <= 64 &&
+         (Ls & (Ls - 1)) == 0;
+}
+
 DhopParams make_params(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in) {
   DhopParams p;
   p.U = g->d;
@@ -102,6 +108,15 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
   p.mf = mf;
   p.khop = khop;
   if (ex) p.c5 = ex->c5;
+  if (ex && ex->mobius) {
+    if (!dag || epi != 1 || ex->r || !mobius_fusable(g, in)) {
+      set_error("fused Mobius adjoint: DhopDag with the M epilogue, FP32, one right-hand side, Ls a power of two <= 64");
+      return GBDW_ERR_INVALID;
+    }
+    p.mob = 1;
+    p.mb = ex->mb;
+    p.mc = ex->mc;
+  }
   if (cen) {
     p.cen = cen->d;
     p.cen_norm = cen->norm;
@@ -119,6 +134,7 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
   }
   DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, tune_epi);
   if (in->LsE % L.spt != 0) L.spt = 1;
+  if (p.mob) L.spt = 2;  // the fused adjoint works on slice pairs, one site's pairs in consecutive lanes
   int NS = 0, tthreads = 0;
   size_t smem = 0;
   const bool staged = L.mode == 1 || L.mode == 2;

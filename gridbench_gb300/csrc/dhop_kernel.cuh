@@ -426,6 +426,11 @@ struct DhopParams {
   float* r_norm = nullptr;  // EPI 4: FP16 r with per-slice norms
   int rLsP = 0;
   const double* alpha = nullptr;
+  // Mobius adjoint (EPI 1, DhopDag, FP32 slice pairs, one right-hand side, Ls a power of two <= 64):
+  // the hopping result v is replaced by A(mb, mc)^dag v before the M epilogue, so the launch
+  // computes Mooee^dag in - khop A(b, c)^dag DhopDag in in one pass
+  int mob = 0;
+  double mb = 1.0, mc = 0.0;
 };
 
 // Writes N slices of v[N][12] (slices e0.., norms for F16); returns the sum of squares of
@@ -557,6 +562,46 @@ __device__ __forceinline__ void dwf_epilogue(const DhopParams& p, int64_t site, 
   }
 }
 
+// ------------------------------------------------------------------ Mobius 5th-dimension adjoint
+// v <- A(b, c)^dag v on one thread's slice pair (s0, s0+1):
+//   (A^dag v)(s) = b v(s) + c [w_lo(s) P- v(s-1) + w_hi(s) P+ v(s+1)],
+// w_lo(0) = w_hi(Ls-1) = -mf, 1 elsewhere.  The Ls/2 threads of a site hold its slices in
+// consecutive lanes (pairs in order), so P- v(s0-1) is the second slice of the lane below and
+// P+ v(s0+2) the first slice of the lane above, both taken with shuffles inside the site's
+// group of lanes (which wraps around the 5th dimension).  Every site's lanes are active or
+// inactive together.
+template <class T>
+__device__ __forceinline__ void mobius_adj_hop(const DhopParams& p, int s0, cpx<T> (&v)[2][12]) {
+  const int G = p.Ls >> 1;  // lanes per site: a power of two <= 32
+  const unsigned mask = __activemask();
+  const int lg = int(threadIdx.x) & (G - 1);
+  const int from_lo = (lg + G - 1) & (G - 1);
+  const int from_hi = (lg + 1) & (G - 1);
+  cpx<T> vm[6], vp[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    vm[k] = {__shfl_sync(mask, v[1][6 + k].r, from_lo, G), __shfl_sync(mask, v[1][6 + k].i, from_lo, G)};
+    vp[k] = {__shfl_sync(mask, v[0][k].r, from_hi, G), __shfl_sync(mask, v[0][k].i, from_hi, G)};
+  }
+  const T b = T(p.mb), c = T(p.mc);
+  const T clo = s0 == 0 ? T(-p.mf) * c : c;           // slice s0: its s-1 wraps at the wall
+  const T chi = s0 + 2 == p.Ls ? T(-p.mf) * c : c;    // slice s0+1: its s+1 wraps at the wall
+  cpx<T> h[2][12];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    // P+ (spins 0, 1) from s+1
+    h[0][k] = {b * v[0][k].r + c * v[1][k].r, b * v[0][k].i + c * v[1][k].i};
+    h[1][k] = {b * v[1][k].r + chi * vp[k].r, b * v[1][k].i + chi * vp[k].i};
+    // P- (spins 2, 3) from s-1
+    h[0][6 + k] = {b * v[0][6 + k].r + clo * vm[k].r, b * v[0][6 + k].i + clo * vm[k].i};
+    h[1][6 + k] = {b * v[1][6 + k].r + c * v[0][6 + k].r, b * v[1][6 + k].i + c * v[0][6 + k].i};
+  }
+#pragma unroll
+  for (int j = 0; j < 2; ++j)
+#pragma unroll
+    for (int k = 0; k < 12; ++k) v[j][k] = h[j][k];
+}
+
 // ------------------------------------------------------------------ per-site finish
 // EPI 0: store Dhop(in); EPI 1: store M(in); EPI 2 / 3 / 4: r -= alpha M(in) with r FP32 / FP64 /
 // FP16 (the CG residual update fused into the operator's second pass; M(in) is not stored).
@@ -564,6 +609,9 @@ __device__ __forceinline__ void dwf_epilogue(const DhopParams& p, int64_t site, 
 template <int PIN, int POUT, int DAG, int N, int EPI, class T>
 __device__ __forceinline__ void finish_site(const DhopParams& p, int64_t site, int s0, int LsE, int LsP,
                                             cpx<T> (&v)[N][12], float& part, double& dpart) {
+  if constexpr (EPI == 1 && DAG == 1 && N == 2 && PIN == GBDW_F32) {
+    if (p.mob) mobius_adj_hop(p, s0, v);
+  }
   if constexpr (EPI >= 1) dwf_epilogue<PIN, DAG, N>(p, site, s0, v);
   if constexpr (EPI == 4) {
     // FP16 r: dequantise with its per-slice norms, update in FP32, store with new norms

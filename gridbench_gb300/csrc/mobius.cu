@@ -444,6 +444,15 @@ int mobius_m(const gbdw_gauge* g, gbdw_field* out, gbdw_field* tmp, const gbdw_f
     ex.c5 = m.cee();
     return run_dhop(g, out, tmp, 0, 1, m.bee(), m.mf, norm2, true, in, 0.5, &ex);
   }
+  if (mobius_fusable(g, in)) {
+    // one pass: out = Mooee^dag in - 1/2 A(b, c)^dag DhopDag in, A^dag applied in the epilogue
+    DhopExtra ex;
+    ex.c5 = m.cee();
+    ex.mobius = true;
+    ex.mb = m.b;
+    ex.mc = m.c;
+    return run_dhop(g, out, in, 1, 1, m.bee(), m.mf, norm2, true, nullptr, 0.5, &ex);
+  }
   // tmp = DhopDag in;  out = Mooee^dag in + (-1/2 A(b, c))^dag tmp
   if (int st = run_dhop(g, tmp, in, 1, 0, 0.0, 0.0, nullptr)) return st;
   const Coef5 b5 = meo5(Ls, m, -0.5);

@@ -237,3 +237,45 @@ def test_mobius_eo_solver(gpu, mode, sp):
         y = gb.Field(lat, gb.F64)
         gb.cg_solve_mobius(g[gb.F64], y, rhs, B5, C5, M5, MF, gb.CG_DOUBLE, tol=1e-12, max_iter=5000)
         assert rel_err(xv, y.numpy()) < 1e-7
+
+
+FORMS_LS16 = [(128, 2, 0, 4), (64, 2, 3, 4), (128, 2, 4, 4), (64, 2, 2, 2), (128, 2, 1, 2), (64, 4, 0, 4)]
+
+
+@pytest.mark.parametrize("Ls", [2, 4, 8, 16, 32])
+def test_mobius_adjoint_fused_pass_every_form(gpu, Ls):
+    """M^dag in one hopping pass (A(b, c)^dag applied in the epilogue with lane shuffles, FP32,
+    Ls a power of two) against the oracle, in every launch form the tuner may pick, with the
+    fused norm; a periodic lattice so the blocked form applies at Ls = 16."""
+    dims = (4, 2, 4, 2)
+    c = make_case(dims, Ls)
+    lat = gb.Lattice.periodic(dims, Ls)
+    g = gb.Gauge(lat, c["U"], gb.F32)
+    x = gb.Field(lat, gb.F32).load(c["phi"])
+    y, t = gb.Field(lat, gb.F32), gb.Field(lat, gb.F32)
+    ref = mob.mobius_m(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], Ls, B5, C5, M5, MF, 1)
+    shapes = FORMS_LS16 if Ls == 16 else [(128, 2, 0, 4), (64, 2, 2, 2), (128, 1, 0, 4)]
+    for shape in shapes:
+        try:
+            gb.tune_set(g, x, *shape)
+        except gb.GbdwError:
+            continue
+        y.zero()
+        n2 = gb.mobius_m(g, y, t, x, B5, C5, M5, MF, 1, want_norm=True)
+        out = y.numpy()
+        assert rel_err(out, ref) < TOL[gb.F32], shape
+        assert abs(n2 - float(np.sum(out ** 2))) / n2 < 1e-5, shape
+    gb.synchronize()
+
+
+def test_mobius_adjoint_unfused_extents(gpu):
+    """Ls = 6 (not a power of two) and 2 right-hand sides keep the two-pass adjoint."""
+    for Ls in (6, 12):
+        c = make_case((2, 2, 4, 2), Ls)
+        lat = gb.Lattice.from_table(c["nbr"], c["prm"], c["nsite"], Ls)
+        g = gb.Gauge(lat, c["U"], gb.F32)
+        x = gb.Field(lat, gb.F32).load(c["phi"])
+        y, t = gb.Field(lat, gb.F32), gb.Field(lat, gb.F32)
+        gb.mobius_m(g, y, t, x, B5, C5, M5, MF, 1)
+        ref = mob.mobius_m(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], Ls, B5, C5, M5, MF, 1)
+        assert rel_err(y.numpy(), ref) < TOL[gb.F32], Ls
