@@ -109,13 +109,14 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
   p.khop = khop;
   if (ex) p.c5 = ex->c5;
   if (ex && ex->mobius) {
-    if (!dag || epi != 1 || ex->r || !mobius_fusable(g, in)) {
-      set_error("fused Mobius adjoint: DhopDag with the M epilogue, FP32, one right-hand side, Ls a power of two <= 64");
+    if (epi != 1 || ex->r || !mobius_fusable(g, in)) {
+      set_error("fused Mobius operator: the M epilogue, FP32, one right-hand side, Ls a power of two <= 64");
       return GBDW_ERR_INVALID;
     }
     p.mob = 1;
     p.mb = ex->mb;
     p.mc = ex->mc;
+    if (!dag) epi = 6;  // A(b, c) on the neighbours as they are loaded; the adjoint's is in the epilogue
   }
   if (cen) {
     p.cen = cen->d;

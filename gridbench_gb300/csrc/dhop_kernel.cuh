@@ -225,9 +225,47 @@ __device__ __forceinline__ cp2 hproj(uint2 x, uint2 y) {
   return {__half22float2(r), __half22float2(i)};
 }
 
-template <int PIN, int DAG, int NP, int L, bool SMEM>
+// Mobius A(b, c) applied to a neighbour's slice pair (s0, s0+1) as it is loaded (the forward
+// Mobius M: the hopping term acts on A(b, c) psi):
+//   (A psi)(s) = b psi(s) + c [w_hi(s) P- psi(s+1) + w_lo(s) P+ psi(s-1)],
+// w_lo(0) = w_hi(Ls-1) = -mf.  The site's Ls/2 lanes load the same neighbour's pairs in order,
+// so psi(s0-1) is the second slice of the lane below and psi(s0+2) the first slice of the lane
+// above (shuffles inside the site's group of lanes, which wraps around the 5th dimension).
+struct MobLeg {
+  float b, c, clo, chi;  // clo: coefficient of slice s0's s-1 term, chi: of slice s0+1's s+1 term
+  int G, from_lo, from_hi;
+};
+__device__ __forceinline__ MobLeg make_mobleg(int Ls, double b, double c, double mf, int s0) {
+  MobLeg m;
+  m.G = Ls >> 1;
+  const int lg = int(threadIdx.x) & (m.G - 1);
+  m.from_lo = (lg + m.G - 1) & (m.G - 1);
+  m.from_hi = (lg + 1) & (m.G - 1);
+  m.b = float(b);
+  m.c = float(c);
+  m.clo = s0 == 0 ? float(-mf * c) : float(c);
+  m.chi = s0 + 2 == Ls ? float(-mf * c) : float(c);
+  return m;
+}
+// spins 0, 1 (P+): slice s0 takes psi(s0-1) from the lane below, slice s0+1 takes psi(s0)
+__device__ __forceinline__ void mob_lower(cp2& a, const MobLeg& m) {
+  const unsigned mask = __activemask();
+  const float mr = __shfl_sync(mask, a.r.y, m.from_lo, m.G), mi = __shfl_sync(mask, a.i.y, m.from_lo, m.G);
+  a.r = __ffma2_rn(make_float2(m.b, m.b), a.r, make_float2(m.clo * mr, m.c * a.r.x));
+  a.i = __ffma2_rn(make_float2(m.b, m.b), a.i, make_float2(m.clo * mi, m.c * a.i.x));
+}
+// spins 2, 3 (P-): slice s0 takes psi(s0+1), slice s0+1 takes psi(s0+2) from the lane above
+__device__ __forceinline__ void mob_upper(cp2& a, const MobLeg& m) {
+  const unsigned mask = __activemask();
+  const float qr = __shfl_sync(mask, a.r.x, m.from_hi, m.G), qi = __shfl_sync(mask, a.i.x, m.from_hi, m.G);
+  a.r = __ffma2_rn(make_float2(m.b, m.b), a.r, make_float2(m.c * a.r.y, m.chi * qr));
+  a.i = __ffma2_rn(make_float2(m.b, m.b), a.i, make_float2(m.c * a.i.y, m.chi * qi));
+}
+
+template <int PIN, int DAG, int NP, int L, bool SMEM, bool MOB = false>
 __device__ __forceinline__ void hop_leg_pairs(const cpx<float> (&u)[3][3], const void* in, int64_t row0, int e0,
-                                              int LsP, const float* nrm, cp2 (&acc)[NP][12]) {
+                                              int LsP, const float* nrm, cp2 (&acc)[NP][12],
+                                              const MobLeg* ml = nullptr) {
   using S = LegSpin<DAG ? (L ^ 4) : L>;
   cp2 h0[NP][3], h1[NP][3];
 #pragma unroll
@@ -249,6 +287,12 @@ __device__ __forceinline__ void hop_leg_pairs(const cpx<float> (&u)[3][3], const
       Vec<PIN, 2 * NP, SMEM>::load_pairs(in, row0 + S::A * 3 + c, e0, LsP, y);
       Vec<PIN, 2 * NP, SMEM>::load_pairs(in, row0 + 1 * 3 + c, e0, LsP, z);
       Vec<PIN, 2 * NP, SMEM>::load_pairs(in, row0 + S::B * 3 + c, e0, LsP, w);
+      if constexpr (MOB && NP == 1) {
+        mob_lower(x[0], *ml);  // spin 0
+        mob_lower(z[0], *ml);  // spin 1
+        mob_upper(y[0], *ml);  // spin A (2 or 3)
+        mob_upper(w[0], *ml);  // spin B (3 or 2)
+      }
 #pragma unroll
       for (int q = 0; q < NP; ++q) {
         h0[q][c] = cadd2(x[q], cunit2<S::C0>(y[q]));
@@ -385,10 +429,11 @@ struct Acc {
   }
 };
 
-template <int PIN, int DAG, int N, int L, bool SMEM>
+template <int PIN, int DAG, int N, int L, bool SMEM, bool MOB = false>
 __device__ __forceinline__ void hop_leg(const cpx<typename Arith<PIN>::T> (&u)[3][3], const void* in, int64_t row0,
-                                        int e0, int LsP, const float* nrm, Acc<PIN, N>& acc) {
-  if constexpr (Acc<PIN, N>::paired) hop_leg_pairs<PIN, DAG, N / 2, L, SMEM>(u, in, row0, e0, LsP, nrm, acc.v);
+                                        int e0, int LsP, const float* nrm, Acc<PIN, N>& acc,
+                                        const MobLeg* ml = nullptr) {
+  if constexpr (Acc<PIN, N>::paired) hop_leg_pairs<PIN, DAG, N / 2, L, SMEM, MOB>(u, in, row0, e0, LsP, nrm, acc.v, ml);
   else hop_leg_scalar<PIN, DAG, N, L, SMEM>(u, in, row0, e0, LsP, nrm, acc.v);
 }
 
@@ -604,7 +649,8 @@ __device__ __forceinline__ void mobius_adj_hop(const DhopParams& p, int s0, cpx<
 
 // ------------------------------------------------------------------ per-site finish
 // EPI 0: store Dhop(in); EPI 1: store M(in); EPI 2 / 3 / 4: r -= alpha M(in) with r FP32 / FP64 /
-// FP16 (the CG residual update fused into the operator's second pass; M(in) is not stored).
+// FP16 (the CG residual update fused into the operator's second pass; M(in) is not stored);
+// EPI 6: store the Mobius M(in), A(b, c) applied to the neighbours as they are loaded.
 // Returns |what was stored|^2 in part (FP32 outputs) or dpart (FP64 outputs and EPI 2-4).
 template <int PIN, int POUT, int DAG, int N, int EPI, class T>
 __device__ __forceinline__ void finish_site(const DhopParams& p, int64_t site, int s0, int LsE, int LsP,
@@ -628,7 +674,7 @@ __device__ __forceinline__ void finish_site(const DhopParams& p, int64_t site, i
         rv[j][k] = {fmaf(-al, float(v[j][k].r), x[j].r * nr[j]), fmaf(-al, float(v[j][k].i), x[j].i * nr[j])};
     }
     dpart = double(store_spinor<GBDW_F16, N>(p.r, p.r_norm, site, s0, LsE, p.rLsP, rv));
-  } else if constexpr (EPI >= 2) {
+  } else if constexpr (EPI == 2 || EPI == 3) {
     constexpr int RP = EPI == 2 ? GBDW_F32 : GBDW_F64;
     using TR = typename Arith<RP>::T;
     const TR al = TR(*p.alpha);
@@ -656,19 +702,21 @@ __device__ __forceinline__ void finish_site(const DhopParams& p, int64_t site, i
 
 // ------------------------------------------------------------------ kernels
 // Hopping sum for one thread: site and first slice s0 of N consecutive slices.
-template <int PIN, int GP, int DAG, int N>
+template <int PIN, int GP, int DAG, int N, bool MOB = false>
 __device__ __forceinline__ void dhop_thread(const DhopParams& p, unsigned site, int s0,
                                             cpx<typename Arith<PIN>::T> (&out)[N][12]) {
   using T = typename Arith<PIN>::T;
   Acc<PIN, N> acc;
   acc.zero();
   const uint32_t* nb = p.nbr4 + size_t(site) * 8;
+  MobLeg ml;
+  if constexpr (MOB) ml = make_mobleg(p.Ls, p.mb, p.mc, p.mf, s0);
 #define GBDW_LEG(L)                                                                                    \
   {                                                                                                    \
     const int64_t n = __ldg(nb + L);                                                                   \
     cpx<T> u[3][3];                                                                                    \
     LinkIO<GP>::load(p.U, size_t(site) * 8 + L, u);                                                    \
-    hop_leg<PIN, DAG, N, L, false>(u, p.in, n * 12, s0, p.LsP, p.in_norm + n * p.LsE + s0, acc);       \
+    hop_leg<PIN, DAG, N, L, false, MOB>(u, p.in, n * 12, s0, p.LsP, p.in_norm + n * p.LsE + s0, acc, &ml); \
   }
   // each forward leg next to its backward partner: the x-neighbours of a CTA's sites are the
   // CTA's own sites, and a spinor one thread reads for X+ is read again for X- by the thread
@@ -717,11 +765,11 @@ __global__ void __launch_bounds__(MINB > 0 ? MAXT : 256, MINB > 0 ? MINB : 1) k_
       site = x + unsigned(p.dims[0]) * (y + unsigned(p.dims[1]) * (z + unsigned(p.dims[2]) * t));
     }
     cpx<T> acc[N][12];
-    dhop_thread<PIN, GP, DAG, N>(p, site, s0, acc);
+    dhop_thread<PIN, GP, DAG, N, EPI == 6>(p, site, s0, acc);
     finish_site<PIN, POUT, DAG, N, EPI>(p, site, s0, p.LsE, p.LsP, acc, part, dpart);
   }
   if (p.partials) {
-    double v[1] = {(POUT == GBDW_F64 || EPI >= 2) ? dpart : double(part)};
+    double v[1] = {(POUT == GBDW_F64 || (EPI >= 2 && EPI <= 4)) ? dpart : double(part)};
     block_partial<1>(v, p.partials);
   }
 }

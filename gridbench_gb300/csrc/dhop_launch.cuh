@@ -126,9 +126,18 @@ int by_shape(const DhopParams& p, DhopLaunch L) {
 }
 
 // epi 0 Dhop, 1 M; the CG residual epilogues exist for the adjoint pass only: 2 (FP32 r, FP32
-// and FP16 spinors), 3 (FP64 r, FP32 spinors) and 4 (FP16 r, FP16 spinors with FP16 links).
+// and FP16 spinors), 3 (FP64 r, FP32 spinors) and 4 (FP16 r, FP16 spinors with FP16 links);
+// 6 the forward Mobius M (FP32).
 template <int PIN, int POUT, int GP, int S1, int S2>
 int dispatch(const DhopParams& p, int dag, int epi, DhopLaunch L) {
+  if (epi == 6) {
+    // the forward Mobius M (A(b, c) on the loaded neighbours): FP32 slice pairs only
+    if constexpr (PIN == GBDW_F32) {
+      if (!dag && L.spt == 2) return by_shape<PIN, POUT, GP, 0, 6, S1, S2>(p, L);
+    }
+    set_error("hopping kernel: the fused Mobius M needs FP32 slice pairs and the forward operator");
+    return GBDW_ERR_INVALID;
+  }
   if (epi >= 2) {
     if constexpr (PIN == GBDW_F32 || PIN == GBDW_F16) {
       if (dag && epi == 2) return by_shape<PIN, POUT, GP, 1, 2, S1, S2>(p, L);

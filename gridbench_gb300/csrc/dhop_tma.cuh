@@ -127,6 +127,8 @@ __global__ void __launch_bounds__(256) k_dhop_tma(const DhopParams p, int NS) {
 
   Acc<PIN, N> acc;
   acc.zero();
+  MobLeg ml;
+  if constexpr (EPI == 6) ml = make_mobleg(p.Ls, p.mb, p.mc, p.mf, s0);
 
   int consumed = 0;  // legs whose stage has been waited for
   bool failed = __syncthreads_or(!mbar_wait_bounded(&bars[STAGES], 0, kWaitLimitNs));
@@ -142,8 +144,8 @@ __global__ void __launch_bounds__(256) k_dhop_tma(const DhopParams p, int NS) {
       if (active) {                                                                                         \
         cpx<T> u[3][3];                                                                                     \
         LinkIO<GP>::template load<true>(my_links, (L), u);                                                  \
-        hop_leg<PIN, DAG, N, L, true>(u, base + sl * blk, 0, s0, LsP,                                       \
-                                      reinterpret_cast<const float*>(base + NS * blk + sl * nblk) + s0, acc); \
+        hop_leg<PIN, DAG, N, L, true, EPI == 6>(u, base + sl * blk, 0, s0, LsP,                             \
+                                      reinterpret_cast<const float*>(base + NS * blk + sl * nblk) + s0, acc, &ml); \
       }                                                                                                     \
       if ((L) + STAGES < 8) {                                                                               \
         __syncthreads();                                                                                    \
@@ -172,7 +174,7 @@ __global__ void __launch_bounds__(256) k_dhop_tma(const DhopParams p, int NS) {
   }
   if (p.partials) {
     // also reached after a timeout, so every block's partial is written
-    double v[1] = {(POUT == GBDW_F64 || EPI >= 2) ? dpart : double(part)};
+    double v[1] = {(POUT == GBDW_F64 || (EPI >= 2 && EPI <= 4)) ? dpart : double(part)};
     block_partial<1>(v, p.partials);
   }
 }
@@ -221,6 +223,8 @@ __global__ void __launch_bounds__(256) k_dhop_tmaw(const DhopParams p_) {
 
   Acc<PIN, N> acc;
   acc.zero();
+  MobLeg ml;
+  if constexpr (EPI == 6) ml = make_mobleg(p.Ls, p.mb, p.mc, p.mf, s0);
   bool failed = false;
   int consumed = 0;
 
@@ -266,8 +270,8 @@ __global__ void __launch_bounds__(256) k_dhop_tmaw(const DhopParams p_) {
       if (active) {                                                                                        \
         cpx<T> u[3][3];                                                                                    \
         LinkIO<GP>::template load<true>(my_links, (L), u);                                                 \
-        hop_leg<PIN, DAG, N, L, true>(u, base + sl * blk, 0, s0, LsP,                                      \
-                                      reinterpret_cast<const float*>(base + NSW * blk + sl * nblk) + s0, acc); \
+        hop_leg<PIN, DAG, N, L, true, EPI == 6>(u, base + sl * blk, 0, s0, LsP,                            \
+                                      reinterpret_cast<const float*>(base + NSW * blk + sl * nblk) + s0, acc, &ml); \
       }                                                                                                    \
       if ((L) + STAGES < 8) {                                                                              \
         __syncwarp();                                                                                      \
@@ -296,7 +300,7 @@ __global__ void __launch_bounds__(256) k_dhop_tmaw(const DhopParams p_) {
     finish_site<PIN, POUT, DAG, N, EPI>(p, site, s0, LsE, LsP, out, part, dpart);
   }
   if (p.partials) {
-    double v[1] = {(POUT == GBDW_F64 || EPI >= 2) ? dpart : double(part)};
+    double v[1] = {(POUT == GBDW_F64 || (EPI >= 2 && EPI <= 4)) ? dpart : double(part)};
     block_partial<1>(v, p.partials);
   }
 }

@@ -23,7 +23,10 @@
 // Kernels: k_m5d (out = A x [+ B y], one thread per 4D site and N slices, every operand read
 // once: HBM bound, 2 spinors per 5D site per operand) and k_m5d_inv (A^-1 as two cyclic
 // bidiagonal solves per chirality, O(Ls) per row, the same two-phase shared-memory tile as the
-// Shamir D5^-1 in eo.cu).
+// Shamir D5^-1 in eo.cu).  For FP32 fields with one right-hand side and Ls a power of two, M and
+// M^dag are single hopping passes instead: A(b, c) is applied to the neighbours' slices as they
+// are loaded, A(b, c)^dag to the hopping result in the epilogue, the neighbouring slices in
+// both cases taken by shuffles from the lanes of the same site (dhop_kernel.cuh).
 #include <cmath>
 #include <string>
 
@@ -437,21 +440,23 @@ int mobius_m(const gbdw_gauge* g, gbdw_field* out, gbdw_field* tmp, const gbdw_f
   if (!check_mobius(m)) return GBDW_ERR_INVALID;
   if (int st = check_ls(in)) return st;
   const int Ls = in->lat->Ls;
+  if (mobius_fusable(g, in)) {
+    // one pass: M in = Mooee in - 1/2 Dhop A(b, c) in with A applied to each neighbour's slices
+    // as they are loaded (dag 0), or M^dag in = Mooee^dag in - 1/2 A(b, c)^dag DhopDag in with
+    // A^dag applied in the epilogue (dag 1)
+    DhopExtra ex;
+    ex.c5 = m.cee();
+    ex.mobius = true;
+    ex.mb = m.b;
+    ex.mc = m.c;
+    return run_dhop(g, out, in, dag, 1, m.bee(), m.mf, norm2, true, nullptr, 0.5, &ex);
+  }
   if (!dag) {
     // tmp = A(b, c) in;  out = Mooee in - 1/2 Dhop tmp  (the hopping epilogue with a5 = bee, c5 = cee)
     if (int st = m5d(tmp, in, meo5(Ls, m, 1.0), nullptr, nullptr, 0)) return st;
     DhopExtra ex;
     ex.c5 = m.cee();
     return run_dhop(g, out, tmp, 0, 1, m.bee(), m.mf, norm2, true, in, 0.5, &ex);
-  }
-  if (mobius_fusable(g, in)) {
-    // one pass: out = Mooee^dag in - 1/2 A(b, c)^dag DhopDag in, A^dag applied in the epilogue
-    DhopExtra ex;
-    ex.c5 = m.cee();
-    ex.mobius = true;
-    ex.mb = m.b;
-    ex.mc = m.c;
-    return run_dhop(g, out, in, 1, 1, m.bee(), m.mf, norm2, true, nullptr, 0.5, &ex);
   }
   // tmp = DhopDag in;  out = Mooee^dag in + (-1/2 A(b, c))^dag tmp
   if (int st = run_dhop(g, tmp, in, 1, 0, 0.0, 0.0, nullptr)) return st;

@@ -243,17 +243,19 @@ FORMS_LS16 = [(128, 2, 0, 4), (64, 2, 3, 4), (128, 2, 4, 4), (64, 2, 2, 2), (128
 
 
 @pytest.mark.parametrize("Ls", [2, 4, 8, 16, 32])
-def test_mobius_adjoint_fused_pass_every_form(gpu, Ls):
-    """M^dag in one hopping pass (A(b, c)^dag applied in the epilogue with lane shuffles, FP32,
-    Ls a power of two) against the oracle, in every launch form the tuner may pick, with the
-    fused norm; a periodic lattice so the blocked form applies at Ls = 16."""
+@pytest.mark.parametrize("dag", [0, 1])
+def test_mobius_fused_pass_every_form(gpu, Ls, dag):
+    """M and M^dag in one hopping pass each (FP32, Ls a power of two): A(b, c) applied to the
+    neighbours' slices as they are loaded, A(b, c)^dag applied in the epilogue, the neighbouring
+    slices taken by lane shuffles; against the oracle in every launch form the tuner may pick,
+    with the fused norm; a periodic lattice so the blocked form applies at Ls = 16."""
     dims = (4, 2, 4, 2)
     c = make_case(dims, Ls)
     lat = gb.Lattice.periodic(dims, Ls)
     g = gb.Gauge(lat, c["U"], gb.F32)
     x = gb.Field(lat, gb.F32).load(c["phi"])
     y, t = gb.Field(lat, gb.F32), gb.Field(lat, gb.F32)
-    ref = mob.mobius_m(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], Ls, B5, C5, M5, MF, 1)
+    ref = mob.mobius_m(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], Ls, B5, C5, M5, MF, dag)
     shapes = FORMS_LS16 if Ls == 16 else [(128, 2, 0, 4), (64, 2, 2, 2), (128, 1, 0, 4)]
     for shape in shapes:
         try:
@@ -261,21 +263,22 @@ def test_mobius_adjoint_fused_pass_every_form(gpu, Ls):
         except gb.GbdwError:
             continue
         y.zero()
-        n2 = gb.mobius_m(g, y, t, x, B5, C5, M5, MF, 1, want_norm=True)
+        n2 = gb.mobius_m(g, y, t, x, B5, C5, M5, MF, dag, want_norm=True)
         out = y.numpy()
         assert rel_err(out, ref) < TOL[gb.F32], shape
         assert abs(n2 - float(np.sum(out ** 2))) / n2 < 1e-5, shape
     gb.synchronize()
 
 
-def test_mobius_adjoint_unfused_extents(gpu):
-    """Ls = 6 (not a power of two) and 2 right-hand sides keep the two-pass adjoint."""
+@pytest.mark.parametrize("dag", [0, 1])
+def test_mobius_unfused_extents(gpu, dag):
+    """Ls = 6 and 12 (not powers of two) keep the two-pass operators."""
     for Ls in (6, 12):
         c = make_case((2, 2, 4, 2), Ls)
         lat = gb.Lattice.from_table(c["nbr"], c["prm"], c["nsite"], Ls)
         g = gb.Gauge(lat, c["U"], gb.F32)
         x = gb.Field(lat, gb.F32).load(c["phi"])
         y, t = gb.Field(lat, gb.F32), gb.Field(lat, gb.F32)
-        gb.mobius_m(g, y, t, x, B5, C5, M5, MF, 1)
-        ref = mob.mobius_m(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], Ls, B5, C5, M5, MF, 1)
+        gb.mobius_m(g, y, t, x, B5, C5, M5, MF, dag)
+        ref = mob.mobius_m(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], Ls, B5, C5, M5, MF, dag)
         assert rel_err(y.numpy(), ref) < TOL[gb.F32], Ls
