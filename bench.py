@@ -468,13 +468,13 @@ def bench_mrhs(gb, peak) -> dict:
             "rel_err_vs_single": err, "rel_err_vs_fp64": err64, "launch": list(gb.tune_query(g, X))}
 
 
-def bench_batch(gb, peak, nrhs_choices=(1,), seed=2024) -> dict:
+def bench_batch(gb, peak, nrhs_choices=(1,), seed=2024, vols=(8, 12, 16, 20, 24)) -> dict:
     """64 instances in one persistent launch replayed from a CUDA graph: 4D volumes uniform over
     {8^4 .. 24^4}, Ls over {8, 12, 16}, FP32 or FP16 storage, right-hand sides from
     nrhs_choices; against the same instances as 64 separate launches, each on its own
     autotuned shape."""
     rng = np.random.default_rng(seed)
-    vols = [8, 12, 16, 20, 24]
+    vols = list(vols)
     keep, G, O, I, spec = [], [], [], [], []
     flops = 0
     sites5 = 0
@@ -843,7 +843,7 @@ def run_only(args) -> dict:
             "shape": list(gb.tune_query(g, xs[0])), "gpu_launches": int(launches)}
 
 
-AUX_ONLY = ("mobius_m", "halo_pack", "batch", "batch_rhs")
+AUX_ONLY = ("mobius_m", "mobius_mdag", "halo_pack", "batch", "batch_rhs", "batch_small")
 
 
 def run_aux_only(args) -> dict:
@@ -853,15 +853,21 @@ def run_aux_only(args) -> dict:
     import gridbench_gb300 as gb
     if args.only.startswith("batch"):
         peak, _ = measured_peak_hbm()
-        return {"workload": args.only, **(bench_batch(gb, peak) if args.only == "batch" else
-                                          bench_batch(gb, peak, (1, 2, 4), seed=2025))}
+        if args.only == "batch":
+            res = bench_batch(gb, peak)
+        elif args.only == "batch_rhs":
+            res = bench_batch(gb, peak, (1, 2, 4), seed=2025)
+        else:  # 64 instances of at most 12^4 (about 1 GB on the device): the profiling case
+            res = bench_batch(gb, peak, vols=(8, 12))
+        return {"workload": args.only, **res}
     lat = gb.Lattice.periodic(DIMS, LS)
     g = gb.Gauge(lat, None, gb.F32, seed=11)
     xs = [gb.Field(lat, gb.F32).gaussian(21 + i) for i in range(4)]
     y, t = gb.Field(lat, gb.F32), gb.Field(lat, gb.F32)
-    if args.only == "mobius_m":
+    if args.only.startswith("mobius_m"):
         gb.tune_dhop(g, y, xs[0])
-        fn = lambda k: gb.mobius_m(g, y, t, xs[k % 2], 1.5, 0.5, 1.8, 0.01)  # noqa: E731
+        dag = 1 if args.only == "mobius_mdag" else 0
+        fn = lambda k: gb.mobius_m(g, y, t, xs[k % 2], 1.5, 0.5, 1.8, 0.01, dag)  # noqa: E731
     else:
         import torch
         bufs = [torch.empty(xs[0].halo_bytes(k // 2), dtype=torch.uint8, device="cuda") for k in range(8)]
