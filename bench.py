@@ -865,7 +865,10 @@ def run_aux_only(args) -> dict:
     xs = [gb.Field(lat, gb.F32).gaussian(21 + i) for i in range(4)]
     y, t = gb.Field(lat, gb.F32), gb.Field(lat, gb.F32)
     if args.only.startswith("mobius_m"):
-        gb.tune_dhop(g, y, xs[0])
+        if args.shape:
+            gb.tune_set(g, xs[0], *(int(v) for v in args.shape.split(",")))
+        else:
+            gb.tune_dhop(g, y, xs[0])
         dag = 1 if args.only == "mobius_mdag" else 0
         fn = lambda k: gb.mobius_m(g, y, t, xs[k % 2], 1.5, 0.5, 1.8, 0.01, dag)  # noqa: E731
     else:
