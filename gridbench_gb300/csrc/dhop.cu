@@ -53,10 +53,12 @@ bool blocked_ok(const gbdw_lattice* lat, const gbdw_field* in) {
   return true;
 }
 
-bool mobius_fusable(const gbdw_gauge* g, const gbdw_field* in) {
+bool mobius_fusable(const gbdw_gauge* g, const gbdw_field* in, int dag) {
   const int Ls = g->lat->Ls;
-  return g->lat->fast && in->prec == GBDW_F32 && in->nrhs == 1 && in->LsE == in->LsP && Ls >= 2 && Ls <= 64 &&
-         (Ls & (Ls - 1)) == 0;
+  // the adjoint (A^dag in the epilogue) in every precision; the forward operator (A on the loaded
+  // neighbours) on FP32 slice pairs
+  return g->lat->fast && (dag || in->prec == GBDW_F32) && in->nrhs == 1 && in->LsE == in->LsP && Ls >= 2 &&
+         Ls <= 64 && (Ls & (Ls - 1)) == 0;
 }
 
 DhopParams make_params(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in) {
@@ -109,8 +111,9 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
   p.khop = khop;
   if (ex) p.c5 = ex->c5;
   if (ex && ex->mobius) {
-    if (epi != 1 || ex->r || !mobius_fusable(g, in)) {
-      set_error("fused Mobius operator: the M epilogue, FP32, one right-hand side, Ls a power of two <= 64");
+    if (epi != 1 || ex->r || !mobius_fusable(g, in, dag)) {
+      set_error("fused Mobius operator: the M epilogue, one right-hand side, Ls a power of two <= 64, FP32 for "
+                "the forward operator");
       return GBDW_ERR_INVALID;
     }
     p.mob = 1;

@@ -471,9 +471,10 @@ struct DhopParams {
   float* r_norm = nullptr;  // EPI 4: FP16 r with per-slice norms
   int rLsP = 0;
   const double* alpha = nullptr;
-  // Mobius adjoint (EPI 1, DhopDag, FP32 slice pairs, one right-hand side, Ls a power of two <= 64):
-  // the hopping result v is replaced by A(mb, mc)^dag v before the M epilogue, so the launch
-  // computes Mooee^dag in - khop A(b, c)^dag DhopDag in in one pass
+  // Mobius operator in one pass (one right-hand side, Ls a power of two <= 64, two slices per
+  // thread): with EPI 1 and DhopDag the hopping result v is replaced by A(mb, mc)^dag v before the
+  // M epilogue (Mooee^dag in - khop A(b, c)^dag DhopDag in); with EPI 6 (FP32) A(mb, mc) is
+  // applied to the neighbours as they are loaded (Mooee in - khop Dhop A(b, c) in)
   int mob = 0;
   double mb = 1.0, mc = 0.0;
 };
@@ -655,7 +656,7 @@ __device__ __forceinline__ void mobius_adj_hop(const DhopParams& p, int s0, cpx<
 template <int PIN, int POUT, int DAG, int N, int EPI, class T>
 __device__ __forceinline__ void finish_site(const DhopParams& p, int64_t site, int s0, int LsE, int LsP,
                                             cpx<T> (&v)[N][12], float& part, double& dpart) {
-  if constexpr (EPI == 1 && DAG == 1 && N == 2 && PIN == GBDW_F32) {
+  if constexpr (EPI == 1 && DAG == 1 && N == 2) {
     if (p.mob) mobius_adj_hop(p, s0, v);
   }
   if constexpr (EPI >= 1) dwf_epilogue<PIN, DAG, N>(p, site, s0, v);

@@ -23,10 +23,10 @@
 // Kernels: k_m5d (out = A x [+ B y], one thread per 4D site and N slices, every operand read
 // once: HBM bound, 2 spinors per 5D site per operand) and k_m5d_inv (A^-1 as two cyclic
 // bidiagonal solves per chirality, O(Ls) per row, the same two-phase shared-memory tile as the
-// Shamir D5^-1 in eo.cu).  For FP32 fields with one right-hand side and Ls a power of two, M and
-// M^dag are single hopping passes instead: A(b, c) is applied to the neighbours' slices as they
-// are loaded, A(b, c)^dag to the hopping result in the epilogue, the neighbouring slices in
-// both cases taken by shuffles from the lanes of the same site (dhop_kernel.cuh).
+// Shamir D5^-1 in eo.cu).  With one right-hand side and Ls a power of two, M^dag is a single
+// hopping pass in every precision (A(b, c)^dag applied to the hopping result in the epilogue),
+// and so is M for FP32 fields (A(b, c) applied to the neighbours' slices as they are loaded);
+// the neighbouring slices are taken by shuffles from the lanes of the same site (dhop_kernel.cuh).
 #include <cmath>
 #include <string>
 
@@ -440,7 +440,7 @@ int mobius_m(const gbdw_gauge* g, gbdw_field* out, gbdw_field* tmp, const gbdw_f
   if (!check_mobius(m)) return GBDW_ERR_INVALID;
   if (int st = check_ls(in)) return st;
   const int Ls = in->lat->Ls;
-  if (mobius_fusable(g, in)) {
+  if (mobius_fusable(g, in, dag)) {
     // one pass: M in = Mooee in - 1/2 Dhop A(b, c) in with A applied to each neighbour's slices
     // as they are loaded (dag 0), or M^dag in = Mooee^dag in - 1/2 A(b, c)^dag DhopDag in with
     // A^dag applied in the epilogue (dag 1)
@@ -575,15 +575,28 @@ int mobius_mdagm(const gbdw_gauge* g, gbdw_field* out, gbdw_field* t, gbdw_field
   if (!check_mobius(m)) return GBDW_ERR_INVALID;
   if (int st = check_ls(in)) return st;
   const int Ls = in->lat->Ls;
-  // t = M in with |t|^2 reduced in the hopping pass and read after the adjoint passes
-  if (int st = m5d(tmp, in, meo5(Ls, m, 1.0), nullptr, nullptr, 0)) return st;
+  // t = M in with |t|^2 reduced in the hopping pass and read after the adjoint passes (which
+  // reduce nothing)
   DhopExtra ex;
   ex.c5 = m.cee();
   double dummy = 0.0;
-  if (int st = run_dhop(g, t, tmp, 0, 1, m.bee(), m.mf, pap ? &dummy : nullptr, false, in, 0.5, &ex)) return st;
-  if (int st = run_dhop(g, tmp, t, 1, 0, 0.0, 0.0, nullptr)) return st;
-  const Coef5 b5 = meo5(Ls, m, -0.5);
-  if (int st = m5d(out, t, mooee(Ls, m), tmp, &b5, 1)) return st;
+  DhopExtra fx = ex;
+  fx.mobius = true;
+  fx.mb = m.b;
+  fx.mc = m.c;
+  if (mobius_fusable(g, in, 0)) {
+    if (int st = run_dhop(g, t, in, 0, 1, m.bee(), m.mf, pap ? &dummy : nullptr, false, nullptr, 0.5, &fx)) return st;
+  } else {
+    if (int st = m5d(tmp, in, meo5(Ls, m, 1.0), nullptr, nullptr, 0)) return st;
+    if (int st = run_dhop(g, t, tmp, 0, 1, m.bee(), m.mf, pap ? &dummy : nullptr, false, in, 0.5, &ex)) return st;
+  }
+  if (mobius_fusable(g, t, 1)) {
+    if (int st = run_dhop(g, out, t, 1, 1, m.bee(), m.mf, nullptr, false, nullptr, 0.5, &fx)) return st;
+  } else {
+    if (int st = run_dhop(g, tmp, t, 1, 0, 0.0, 0.0, nullptr)) return st;
+    const Coef5 b5 = meo5(Ls, m, -0.5);
+    if (int st = m5d(out, t, mooee(Ls, m), tmp, &b5, 1)) return st;
+  }
   if (pap) {
     Reduce red;
     if (int st = reduce_scratch(1, 1, &red)) return st;

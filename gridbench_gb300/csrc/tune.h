@@ -15,8 +15,8 @@ struct DhopExtra {
   double num = 0.0;                 // with alpha_to: alpha_to = num / sum
   double* alpha_to = nullptr;       // device
   double c5 = 1.0;                  // the epilogue's 5th-dimension hopping coefficient
-  // Mobius adjoint: apply A(mb, mc)^dag to DhopDag in before the epilogue (dag 1, epi 1, FP32,
-  // one right-hand side, Ls a power of two <= 64)
+  // Mobius operator in one pass: A(mb, mc) on the loaded neighbours (dag 0, FP32) or A(mb, mc)^dag
+  // on DhopDag in before the epilogue (dag 1); epi 1, one right-hand side, Ls a power of two <= 64
   bool mobius = false;
   double mb = 1.0, mc = 0.0;
 };
@@ -36,6 +36,7 @@ DhopParams make_params(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* i
 bool form3_ok(const gbdw_field* in, int epi, int spt);
 // form 4 (blocked site order) applies: FP32/FP16, Ls*nrhs = 16, periodic lattice, even extents
 bool blocked_ok(const gbdw_lattice* lat, const gbdw_field* in);
-// the Mobius adjoint can be fused into the hopping pass for these operands (DhopExtra::mobius)
-bool mobius_fusable(const gbdw_gauge* g, const gbdw_field* in);
+// the Mobius operator (dag 0) or its adjoint (dag 1) can be fused into the hopping pass for these
+// operands (DhopExtra::mobius)
+bool mobius_fusable(const gbdw_gauge* g, const gbdw_field* in, int dag);
 }  // namespace gbdw

@@ -244,17 +244,19 @@ FORMS_LS16 = [(128, 2, 0, 4), (64, 2, 3, 4), (128, 2, 4, 4), (64, 2, 2, 2), (128
 
 @pytest.mark.parametrize("Ls", [2, 4, 8, 16, 32])
 @pytest.mark.parametrize("dag", [0, 1])
-def test_mobius_fused_pass_every_form(gpu, Ls, dag):
-    """M and M^dag in one hopping pass each (FP32, Ls a power of two): A(b, c) applied to the
-    neighbours' slices as they are loaded, A(b, c)^dag applied in the epilogue, the neighbouring
-    slices taken by lane shuffles; against the oracle in every launch form the tuner may pick,
-    with the fused norm; a periodic lattice so the blocked form applies at Ls = 16."""
+@pytest.mark.parametrize("prec", [gb.F64, gb.F32, gb.F16])
+def test_mobius_fused_pass_every_form(gpu, Ls, dag, prec):
+    """One hopping pass each for M^dag (every precision: A(b, c)^dag applied in the epilogue) and
+    for M (FP32: A(b, c) applied to the neighbours' slices as they are loaded; FP64 and FP16 keep
+    two passes), Ls a power of two, the neighbouring slices taken by lane shuffles; against the
+    oracle in every launch form the tuner may pick, with the fused norm; a periodic lattice so
+    the blocked form applies at Ls = 16."""
     dims = (4, 2, 4, 2)
     c = make_case(dims, Ls)
     lat = gb.Lattice.periodic(dims, Ls)
-    g = gb.Gauge(lat, c["U"], gb.F32)
-    x = gb.Field(lat, gb.F32).load(c["phi"])
-    y, t = gb.Field(lat, gb.F32), gb.Field(lat, gb.F32)
+    g = gb.Gauge(lat, c["U"], prec)
+    x = gb.Field(lat, prec).load(c["phi"])
+    y, t = gb.Field(lat, prec), gb.Field(lat, prec)
     ref = mob.mobius_m(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], Ls, B5, C5, M5, MF, dag)
     shapes = FORMS_LS16 if Ls == 16 else [(128, 2, 0, 4), (64, 2, 2, 2), (128, 1, 0, 4)]
     for shape in shapes:
@@ -265,8 +267,8 @@ def test_mobius_fused_pass_every_form(gpu, Ls, dag):
         y.zero()
         n2 = gb.mobius_m(g, y, t, x, B5, C5, M5, MF, dag, want_norm=True)
         out = y.numpy()
-        assert rel_err(out, ref) < TOL[gb.F32], shape
-        assert abs(n2 - float(np.sum(out ** 2))) / n2 < 1e-5, shape
+        assert rel_err(out, ref) < TOL[prec], shape
+        assert abs(n2 - float(np.sum(out ** 2))) / n2 < (1e-12 if prec == gb.F64 else 1e-5), shape
     gb.synchronize()
 
 
