@@ -75,18 +75,14 @@ __device__ __forceinline__ cpx<float> b2c(unsigned w) {
   const float2 f = __bfloat1622float2(h);
   return {f.x, f.y};
 }
-// conj(a b - c d) in scalar FMAs whose negations fold into the instruction's operands: no
-// register pairs to assemble (the packed form needs duplicated and swapped operands)
+// conj(a b - c d) with each complex product as two packed FMAs on (re, im):
+// a b = a.r (b.r, b.i) + a.i (-b.i, b.r).
 __device__ __forceinline__ cpx<float> cross_conj(cpx<float> a, cpx<float> b, cpx<float> c, cpx<float> d) {
-  float re = a.r * b.r;
-  re = fmaf(-a.i, b.i, re);
-  re = fmaf(-c.r, d.r, re);
-  re = fmaf(c.i, d.i, re);
-  float im = -a.r * b.i;  // -Im(a b - c d)
-  im = fmaf(-a.i, b.r, im);
-  im = fmaf(c.r, d.i, im);
-  im = fmaf(c.i, d.r, im);
-  return {re, im};
+  float2 t = __fmul2_rn(make_float2(a.r, a.r), make_float2(b.r, b.i));
+  t = __ffma2_rn(make_float2(a.i, a.i), make_float2(-b.i, b.r), t);
+  t = __ffma2_rn(make_float2(-c.r, -c.r), make_float2(d.r, d.i), t);
+  t = __ffma2_rn(make_float2(-c.i, -c.i), make_float2(-d.i, d.r), t);
+  return {t.x, -t.y};
 }
 __device__ __forceinline__ void third_row(cpx<float> (&u)[3][3]) {
 #pragma unroll
