@@ -491,6 +491,17 @@ def tune_set(g: Gauge, inp: Field, threads: int, spt: int, form: int = 0, stages
     check(load().gbdw_tune_set(g.h, inp.h, threads, spt, form, stages))
 
 
+def tune_split(g: Gauge, inp: Field) -> int:
+    """Tiles per site (Ls / RHS tiling) of the direct form chosen for fields like inp."""
+    v = C.c_int()
+    check(load().gbdw_tune_split(g.h, inp.h, C.byref(v)))
+    return v.value
+
+
+def tune_set_split(g: Gauge, inp: Field, split: int):
+    check(load().gbdw_tune_set_split(g.h, inp.h, int(split)))
+
+
 def tune_save(path: str):
     check(load().gbdw_tune_save(path.encode()))
 

@@ -121,6 +121,8 @@ PROTOTYPES = {
     "gbdw_tune_save": (_i, [C.c_char_p]),
     "gbdw_tune_query": (_i, [_vp, _vp, C.POINTER(C.c_int)]),
     "gbdw_tune_set": (_i, [_vp, _vp, _i, _i, _i, _i]),
+    "gbdw_tune_split": (_i, [_vp, _vp, C.POINTER(C.c_int)]),
+    "gbdw_tune_set_split": (_i, [_vp, _vp, _i]),
     "gbdw_selftest_wait_timeout": (_i, [_u64]),
     "gbdw_timer_create": (_i, [_pp]),
     "gbdw_timer_start": (_i, [_vp]),

@@ -53,6 +53,12 @@ bool blocked_ok(const gbdw_lattice* lat, const gbdw_field* in) {
   return true;
 }
 
+int tile_extent(int LsE, const DhopLaunch& L, bool whole_sites) {
+  if (L.split <= 1 || whole_sites || (L.mode != 0 && L.mode != 3) || LsE % L.split) return 0;
+  const int TE = LsE / L.split;
+  return TE % L.spt == 0 ? TE : 0;
+}
+
 bool mobius_fusable(const gbdw_gauge* g, const gbdw_field* in, int dag) {
   const int Ls = g->lat->Ls;
   // the adjoint (A^dag in the epilogue) in every precision; the forward operator (A on the loaded
@@ -148,6 +154,7 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
   if (L.mode == 3 && !form3_ok(in, epi, L.spt)) L.mode = 0;
   if (L.mode == 3) L.threads = 64;
   if (L.mode == 4) L.threads = 128;
+  p.TE = tile_extent(in->LsE, L, p.mob != 0);
   const int64_t nthreads = p.nsite * (p.LsE / L.spt);
   const int64_t blocks = staged ? (p.nsite + NS - 1) / NS : (nthreads + L.threads - 1) / L.threads;
   Reduce red;

@@ -477,6 +477,8 @@ struct DhopParams {
   // applied to the neighbours as they are loaded (Mooee in - khop Dhop A(b, c) in)
   int mob = 0;
   double mb = 1.0, mc = 0.0;
+  // direct forms: slices per tile when each site's slices are cut into tiles (0: one tile)
+  int TE = 0;
 };
 
 // Writes N slices of v[N][12] (slices e0.., norms for F16); returns the sum of squares of
@@ -750,7 +752,19 @@ __global__ void __launch_bounds__(MINB > 0 ? MAXT : 256, MINB > 0 ? MINB : 1) k_
   double dpart = 0.0;
   if (active) {
     unsigned site = tid / G;
-    const int s0 = int(tid - site * G) * N;
+    int s0 = int(tid - site * G) * N;
+    if constexpr (!BLK) {
+      if (p.TE > 0 && p.TE < p.LsE) {
+        // Ls / RHS tiles: threads ordered (tile, site, slice group), TE slices per tile, so a
+        // CTA holds more sites with fewer slices each (the link is reused over one tile)
+        const unsigned GT = unsigned(p.TE) / N;
+        const unsigned per_tile = unsigned(p.nsite) * GT;
+        const unsigned tile = tid / per_tile;
+        const unsigned r = tid - tile * per_tile;
+        site = r / GT;
+        s0 = int(tile) * p.TE + int(r - site * GT) * N;
+      }
+    }
     if constexpr (BLK) {
       const unsigned l = threadIdx.x / G;  // 0..15 inside the block
       const unsigned hx = unsigned(p.dims[0]) >> 1, hy = unsigned(p.dims[1]) >> 1, hz = unsigned(p.dims[2]) >> 1;
@@ -811,6 +825,7 @@ struct DhopLaunch {
                    // 3: direct, FP32/FP16 Ls = 16 at compile time, registers balanced for 6 CTAs/SM
                    // 4: form 3 on 2x2x2x2 site blocks per 128-thread CTA (periodic, even extents)
   int stages = 4;  // staged kernels: depth of the leg ring
+  int split = 1;   // forms 0 and 3: each site's Ls*nrhs slices cut into this many tiles
 };
 
 // Implemented per precision family in dhop_f64.cu / dhop_f32.cu / dhop_f16.cu.

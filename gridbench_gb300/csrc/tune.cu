@@ -1,8 +1,8 @@
 // Autotuner for the hopping kernel: times every admissible launch shape (threads per CTA,
-// slices per thread, form, ring stages) on the caller's own fields with CUDA events and keeps
-// the fastest, keyed by (gauge precision, spinor precision, innermost extent Ls*nrhs,
-// epilogue).  The cache can be written to and read back from a small JSON object
-// {"key": [threads, slices, form, stages], ...}.
+// slices per thread, form, ring stages, and for the direct forms the Ls / RHS tile split) on the
+// caller's own fields with CUDA events and keeps the fastest, keyed by (gauge precision, spinor
+// precision, innermost extent Ls*nrhs, epilogue).  The cache can be written to and read back from
+// a small JSON object {"key": [threads, slices, form, stages, split], ...}.
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -65,7 +65,11 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
   for (int th : threads_c) {
     for (int spt : {1, 2, 4}) {
       if (in->LsE % spt != 0 || (in->prec == GBDW_F64 && spt > 2)) continue;
-      cands.push_back(DhopLaunch{th, spt, 0, 4});
+      // Ls / RHS tiles of the direct form: 1, 2, 4 tiles per site where they cut whole groups
+      for (int split : {1, 2, 4}) {
+        DhopLaunch L{th, spt, 0, 4, split};
+        if (split == 1 || tile_extent(in->LsE, L, false) > 0) cands.push_back(L);
+      }
     }
     for (int mode : {1, 2})
       for (int spt : {s1, s2})
@@ -76,7 +80,10 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
           if (tma_shape(in->prec, in->LsE, L, &ns, &tt, &sm)) cands.push_back(L);
         }
   }
-  if (form3_ok(in, 0, 2)) cands.push_back(DhopLaunch{64, 2, 3, 4});
+  if (form3_ok(in, 0, 2)) {
+    cands.push_back(DhopLaunch{64, 2, 3, 4});
+    if (tile_extent(in->LsE, DhopLaunch{64, 2, 3, 4, 2}, false) > 0) cands.push_back(DhopLaunch{64, 2, 3, 4, 2});
+  }
   if (blocked_ok(g->lat, in)) cands.push_back(DhopLaunch{128, 2, 4, 4});
   cudaEvent_t a, b;
   GBDW_CUDA(cudaEventCreate(&a));
@@ -153,6 +160,26 @@ int gbdw_tune_set(const gbdw_gauge* g, const gbdw_field* in, int threads, int sp
   return GBDW_OK;
 }
 
+int gbdw_tune_split(const gbdw_gauge* g, const gbdw_field* in, int* split) {
+  if (!g || !in || !split) return GBDW_ERR_INVALID;
+  *split = tuned_launch(g->prec, in->prec, in->LsE, 0).split;
+  return GBDW_OK;
+}
+
+int gbdw_tune_set_split(const gbdw_gauge* g, const gbdw_field* in, int split) {
+  if (!g || !in) return GBDW_ERR_INVALID;
+  DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, 0);
+  L.split = split;
+  if (split < 1 || (split > 1 && tile_extent(in->LsE, L, false) == 0)) {
+    set_error("gbdw_tune_set_split: the chosen form must be direct (0 or 3) and Ls*nrhs must split into whole "
+              "slice groups");
+    return GBDW_ERR_INVALID;
+  }
+  set_tuned_launch(g->prec, in->prec, in->LsE, 0, L);
+  if (in->nrhs == 1) set_tuned_launch(g->prec, in->prec, in->LsE, 1, L);
+  return GBDW_OK;
+}
+
 int gbdw_tune_save(const char* path) {
   if (!path) return GBDW_ERR_INVALID;
   FILE* f = fopen(path, "w");
@@ -164,8 +191,8 @@ int gbdw_tune_save(const char* path) {
   fprintf(f, "{");
   bool first = true;
   for (auto& kv : g_tuned) {
-    fprintf(f, "%s\n  \"%s\": [%d, %d, %d, %d]", first ? "" : ",", kv.first.c_str(), kv.second.threads,
-            kv.second.spt, kv.second.mode, kv.second.stages);
+    fprintf(f, "%s\n  \"%s\": [%d, %d, %d, %d, %d]", first ? "" : ",", kv.first.c_str(), kv.second.threads,
+            kv.second.spt, kv.second.mode, kv.second.stages, kv.second.split);
     first = false;
   }
   fprintf(f, "\n}\n");
@@ -185,20 +212,22 @@ int gbdw_tune_load(const char* path) {
   size_t n;
   while ((n = fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, n);
   fclose(f);
-  // Entries look like "g1_s1_L16_e0": [128, 2, 0, 4] (older two-number entries keep form 0)
+  // Entries look like "g1_s1_L16_e0": [128, 2, 0, 4, 1] (threads, slices per thread, form, stages,
+  // tile split; shorter entries keep the defaults of the missing numbers)
   size_t pos = 0;
   int loaded = 0;
   while ((pos = text.find('"', pos)) != std::string::npos) {
     const size_t end = text.find('"', pos + 1);
     if (end == std::string::npos) break;
     const std::string key = text.substr(pos + 1, end - pos - 1);
-    int gp, sp, LsE, epi, th, spt, mode = 0, stages = 4;
+    int gp, sp, LsE, epi, th, spt, mode = 0, stages = 4, split = 1;
     const size_t lb = text.find('[', end);
     if (lb == std::string::npos) break;
     if (sscanf(key.c_str(), "g%d_s%d_L%d_e%d", &gp, &sp, &LsE, &epi) == 4 &&
-        sscanf(text.c_str() + lb, "[%d , %d , %d , %d]", &th, &spt, &mode, &stages) >= 2 && th > 0 && th <= 256 &&
-        th % 32 == 0 && (spt == 1 || spt == 2 || spt == 4) && mode >= 0 && mode <= 4 && (stages == 2 || stages == 4)) {
-      set_tuned_launch(gp, sp, LsE, epi, DhopLaunch{th, spt, mode, stages});
+        sscanf(text.c_str() + lb, "[%d , %d , %d , %d , %d]", &th, &spt, &mode, &stages, &split) >= 2 && th > 0 &&
+        th <= 256 && th % 32 == 0 && (spt == 1 || spt == 2 || spt == 4) && mode >= 0 && mode <= 4 &&
+        (stages == 2 || stages == 4) && split >= 1 && split <= 64) {
+      set_tuned_launch(gp, sp, LsE, epi, DhopLaunch{th, spt, mode, stages, split});
       ++loaded;
     }
     pos = text.find(']', lb);

@@ -36,6 +36,9 @@ DhopParams make_params(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* i
 bool form3_ok(const gbdw_field* in, int epi, int spt);
 // form 4 (blocked site order) applies: FP32/FP16, Ls*nrhs = 16, periodic lattice, even extents
 bool blocked_ok(const gbdw_lattice* lat, const gbdw_field* in);
+// slices per tile of a direct launch with L.split tiles per site, or 0 (one tile: the split does
+// not divide the extent into whole slice groups, a staged or blocked form, or whole_sites)
+int tile_extent(int LsE, const DhopLaunch& L, bool whole_sites);
 // the Mobius operator (dag 0) or its adjoint (dag 1) can be fused into the hopping pass for these
 // operands (DhopExtra::mobius)
 bool mobius_fusable(const gbdw_gauge* g, const gbdw_field* in, int dag);

@@ -329,3 +329,47 @@ def test_fp32_ls12_and_12_rhs_specialised_kernels(gpu, form):
             ref = oracle.dslash(c["U"], srcs[r], c["nbr"], c["prm"], c["nsite"], Ls, dag)
             assert rel_err(Y.numpy(r), ref) < TOL[gb.F32], (dag, r)
     gb.synchronize()
+
+
+@pytest.mark.parametrize("form,threads", [(0, 128), (0, 64), (3, 64)])
+@pytest.mark.parametrize("split", [1, 2, 4])
+def test_direct_forms_with_ls_and_rhs_tiles(gpu, form, threads, split):
+    """Ls / RHS tiles of the direct forms (each site's slices cut into `split` tiles, threads
+    ordered tile, site, group): Dhop, DhopDag and M at Ls = 16 with one right-hand side, and Dhop
+    with 12 right-hand sides at Ls = 12 (form 3 exists there for FP32 Dhop), every rhs against
+    the oracle."""
+    c = make_case((4, 6, 2, 3), 16)
+    lat = gb.Lattice.from_table(c["nbr"], c["prm"], c["nsite"], 16)
+    g = gb.Gauge(lat, c["U"], gb.F32)
+    x, y = gb.Field(lat, gb.F32).load(c["phi"]), gb.Field(lat, gb.F32)
+    gb.tune_set(g, x, threads, 2, form, 4)
+    gb.tune_set_split(g, x, split)
+    assert gb.tune_split(g, x) == split
+    for dag in (0, 1):
+        y.zero()
+        gb.dhop(g, y, x, dag)
+        ref = oracle.dslash(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], 16, dag)
+        assert rel_err(y.numpy(), ref) < TOL[gb.F32], (form, split, dag)
+        n2 = gb.dwf_m(g, y, x, 1.8, 0.01, dag, want_norm=True)
+        refm = oracle.dwf_m(c["U"], c["phi"], c["nbr"], c["nsite"], 16, 1.8, 0.01, dag)
+        out = y.numpy()
+        assert rel_err(out, refm) < TOL[gb.F32], (form, split, dag)
+        assert abs(n2 - float(np.sum(out ** 2))) / n2 < 1e-5
+    # 12 right-hand sides: tiles of 72 / 36 slices (6 / 3 values of s with all 12 rhs)
+    dims, Ls, k = (4, 2, 4, 2), 12, 12
+    c = make_case(dims, Ls)
+    lat = gb.Lattice.from_table(c["nbr"], c["prm"], c["nsite"], Ls)
+    g = gb.Gauge(lat, c["U"], gb.F32)
+    X, Y = gb.Field(lat, gb.F32, k), gb.Field(lat, gb.F32, k)
+    srcs = [gb.generate_fermion(dims, Ls, 1, (5 + r, 6, 7, 8)) for r in range(k)]
+    for r in range(k):
+        X.load(srcs[r], r)
+    gb.tune_set(g, X, threads, 2, form, 4)
+    gb.tune_set_split(g, X, split)
+    gb.dhop(g, Y, X)
+    for r in range(k):
+        ref = oracle.dslash(c["U"], srcs[r], c["nbr"], c["prm"], c["nsite"], Ls)
+        assert rel_err(Y.numpy(r), ref) < TOL[gb.F32], (form, split, r)
+    with pytest.raises(gb.GbdwError):
+        gb.tune_set_split(g, X, 5)  # 144 slices do not cut into 5 tiles
+    gb.synchronize()
