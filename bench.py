@@ -778,9 +778,11 @@ def run_reference(args, D: Dist) -> dict | None:
             "e2e": {"value": round(value, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
-ONLY = {  # name -> (dims, Ls, spinor precision, gauge precision, dag)
+ONLY = {  # name -> (dims, Ls, spinor precision, gauge precision, dag[, right-hand sides])
     "dhop_f32": (DIMS, LS, 1, 1, 0), "dhopdag_f32": (DIMS, LS, 1, 1, 1), "dhop_f64": (DIMS, LS, 0, 0, 0),
     "dhop_f16": (DIMS, LS, 2, 2, 0), "dhop_bf16": (DIMS, LS, 2, 3, 0),
+    # the 12-RHS kernel on a lattice small enough for a full profile (2 x 0.9 GB fields)
+    "dhop_f32_12rhs_16x12": (DIMS, 12, 1, 1, 0, 12),
 }
 
 
@@ -823,11 +825,15 @@ def run_only(args) -> dict:
     ring, 2 TMA-staged warp rings, 3 direct specialised for Ls=16);
     without it the autotuner picks."""
     import gridbench_gb300 as gb
-    dims, Ls, sp, gp, dag = ONLY[args.only]
+    dims, Ls, sp, gp, dag = ONLY[args.only][:5]
+    k = ONLY[args.only][5] if len(ONLY[args.only]) > 5 else 1
     lat = gb.Lattice.periodic(dims, Ls)
     g = gb.Gauge(lat, None, gp, seed=11)
-    xs = [gb.Field(lat, sp).gaussian(21 + i) for i in range(2)]
-    ys = [gb.Field(lat, sp) for _ in range(2)]
+    xs = [gb.Field(lat, sp, k) for _ in range(2)]
+    for i, x in enumerate(xs):
+        for r in range(k):
+            x.gaussian(21 + i + 2 * r, r)
+    ys = [gb.Field(lat, sp, k) for _ in range(2)]
     if args.shape:
         th, spt, form, st = (int(v) for v in args.shape.split(","))
         gb.tune_set(g, xs[0], th, spt, form, st)
@@ -835,12 +841,12 @@ def run_only(args) -> dict:
         gb.tune_dhop(g, ys[0], xs[0], dag)
     ms, launches = time_dhop(gb, g, list(zip(ys, xs)), args.steps, args.warmup, dag)
     gb.synchronize()
-    V5 = int(np.prod(dims)) * Ls
+    V5 = int(np.prod(dims)) * Ls * k
     t = ms / args.steps / 1e3
     peak, _ = measured_peak_hbm()
-    return {"workload": args.only, "lattice": list(dims), "Ls": Ls, "steps": args.steps,
+    return {"workload": args.only, "lattice": list(dims), "Ls": Ls, "rhs": k, "steps": args.steps,
             "us_per_launch": round(t * 1e6, 3), "gflops": round(FLOP_PER_SITE * V5 / t / 1e9, 1),
-            "hbm_frac": round(algo_bytes(sp, gp, Ls) * V5 / t / 1e9 / peak, 4),
+            "hbm_frac": round(algo_bytes(sp, gp, Ls, k) * V5 / t / 1e9 / peak, 4),
             "shape": list(gb.tune_query(g, xs[0])), "gpu_launches": int(launches)}
 
 
