@@ -65,8 +65,10 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
   for (int th : threads_c) {
     for (int spt : {1, 2, 4}) {
       if (in->LsE % spt != 0 || (in->prec == GBDW_F64 && spt > 2)) continue;
-      // Ls / RHS tiles of the direct form: 1, 2, 4 tiles per site where they cut whole groups
-      for (int split : {1, 2, 4}) {
+      // Ls / RHS tiles of the direct form where they cut whole groups: with many right-hand sides
+      // a site's slices are many KB and the reuse distance of its spinor (one 3D volume of sites
+      // along t) can exceed L2; a tile sweep over all sites shortens it by the split factor
+      for (int split : {1, 2, 3, 4, 6, 8, 12, 16}) {
         DhopLaunch L{th, spt, 0, 4, split};
         if (split == 1 || tile_extent(in->LsE, L, false) > 0) cands.push_back(L);
       }
@@ -81,8 +83,10 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
         }
   }
   if (form3_ok(in, 0, 2)) {
-    cands.push_back(DhopLaunch{64, 2, 3, 4});
-    if (tile_extent(in->LsE, DhopLaunch{64, 2, 3, 4, 2}, false) > 0) cands.push_back(DhopLaunch{64, 2, 3, 4, 2});
+    for (int split : {1, 2, 3, 4, 6, 8, 12, 16}) {
+      const DhopLaunch L{64, 2, 3, 4, split};
+      if (split == 1 || tile_extent(in->LsE, L, false) > 0) cands.push_back(L);
+    }
   }
   if (blocked_ok(g->lat, in)) cands.push_back(DhopLaunch{128, 2, 4, 4});
   cudaEvent_t a, b;

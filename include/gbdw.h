@@ -359,8 +359,10 @@ int gbdw_tune_query(const gbdw_gauge* g, const gbdw_field* in, int cfg[4]);
  * 1, 2 or 4 dividing Ls*nrhs, at most 2 for F64; form 0..4; stages 2/4). */
 int gbdw_tune_set(const gbdw_gauge* g, const gbdw_field* in, int threads, int spt, int form, int stages);
 /* Ls / RHS tiles of the direct forms (0 and 3): each site's Ls*nrhs slices are cut into `split`
- * contiguous tiles, threads ordered (tile, site, slice group), so a CTA holds more sites with
- * fewer slices each (one link load per site and tile).  The tuner chooses among 1, 2 and 4;
+ * contiguous tiles, threads ordered (tile, site, slice group), so each tile is one sweep over all
+ * sites: a CTA holds more sites with fewer slices each (one link load per site and tile), and a
+ * site's spinor is reused by its neighbours within a shorter stretch of the sweep.  The tuner
+ * chooses among the splits 1, 2, 3, 4, 6, 8, 12, 16 that cut whole slice groups;
  * gbdw_tune_split reads the choice for fields like `in`, gbdw_tune_set_split pins it (1 = whole
  * sites; gbdw_tune_set resets it to 1). */
 int gbdw_tune_split(const gbdw_gauge* g, const gbdw_field* in, int* split);
