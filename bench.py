@@ -850,7 +850,7 @@ def run_only(args) -> dict:
             "shape": list(gb.tune_query(g, xs[0])), "gpu_launches": int(launches)}
 
 
-AUX_ONLY = ("mobius_m", "mobius_mdag", "halo_pack", "batch", "batch_rhs", "batch_small")
+AUX_ONLY = ("mobius_m", "mobius_mdag", "halo_pack", "batch", "batch_rhs", "batch_small", "mrhs")
 
 
 def run_aux_only(args) -> dict:
@@ -858,6 +858,9 @@ def run_aux_only(args) -> dict:
     eight halo faces, FP32 16^4 x 16, or one of the 64-instance batches, nothing else (for
     profiling)."""
     import gridbench_gb300 as gb
+    if args.only == "mrhs":
+        peak, _ = measured_peak_hbm()
+        return {"workload": "multi_rhs_24^4x12_k12", **bench_mrhs(gb, peak)}
     if args.only.startswith("batch"):
         peak, _ = measured_peak_hbm()
         if args.only == "batch":

@@ -373,3 +373,28 @@ def test_direct_forms_with_ls_and_rhs_tiles(gpu, form, threads, split):
     with pytest.raises(gb.GbdwError):
         gb.tune_set_split(g, X, 5)  # 144 slices do not cut into 5 tiles
     gb.synchronize()
+
+
+@pytest.mark.parametrize("form,threads", [(0, 128), (3, 64)])
+@pytest.mark.parametrize("split", [3, 6, 12, 36])
+def test_multi_rhs_tile_sweeps(gpu, form, threads, split):
+    """12 right-hand sides at Ls = 12 (144 slices per site) in 3 to 36 tile sweeps: tiles of
+    whole values of s (48, 24, 12 slices) and of some right-hand sides at one s (4 slices); every
+    rhs against the oracle, Dhop and DhopDag."""
+    dims, Ls, k = (4, 2, 4, 2), 12, 12
+    c = make_case(dims, Ls)
+    lat = gb.Lattice.from_table(c["nbr"], c["prm"], c["nsite"], Ls)
+    g = gb.Gauge(lat, c["U"], gb.F32)
+    X, Y = gb.Field(lat, gb.F32, k), gb.Field(lat, gb.F32, k)
+    srcs = [gb.generate_fermion(dims, Ls, 1, (5 + r, 6, 7, 8)) for r in range(k)]
+    for r in range(k):
+        X.load(srcs[r], r)
+    gb.tune_set(g, X, threads, 2, form, 4)
+    gb.tune_set_split(g, X, split)
+    for dag in (0, 1):
+        Y.zero()
+        gb.dhop(g, Y, X, dag)
+        for r in range(k):
+            ref = oracle.dslash(c["U"], srcs[r], c["nbr"], c["prm"], c["nsite"], Ls, dag)
+            assert rel_err(Y.numpy(r), ref) < TOL[gb.F32], (form, split, dag, r)
+    gb.synchronize()
