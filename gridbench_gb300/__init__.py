@@ -502,6 +502,17 @@ def tune_set_split(g: Gauge, inp: Field, split: int):
     check(load().gbdw_tune_set_split(g.h, inp.h, int(split)))
 
 
+def tune_brick(g: Gauge, inp: Field) -> int:
+    """t-brick sweep order of the direct form chosen for fields like inp (1: natural order)."""
+    v = C.c_int()
+    check(load().gbdw_tune_brick(g.h, inp.h, C.byref(v)))
+    return v.value
+
+
+def tune_set_brick(g: Gauge, inp: Field, brick: int):
+    check(load().gbdw_tune_set_brick(g.h, inp.h, int(brick)))
+
+
 def tune_save(path: str):
     check(load().gbdw_tune_save(path.encode()))
 

@@ -59,6 +59,13 @@ int tile_extent(int LsE, const DhopLaunch& L, bool whole_sites) {
   return TE % L.spt == 0 ? TE : 0;
 }
 
+int brick_extent(const gbdw_lattice* lat, const DhopLaunch& L) {
+  if (L.brick <= 1 || (L.mode != 0 && L.mode != 3) || lat->parity >= 0 || !lat->fast) return 0;
+  for (int d = 0; d < 4; ++d)
+    if (lat->dims[d] <= 0) return 0;
+  return lat->dims[3] % L.brick == 0 ? L.brick : 0;
+}
+
 bool mobius_fusable(const gbdw_gauge* g, const gbdw_field* in, int dag) {
   const int Ls = g->lat->Ls;
   // the adjoint (A^dag in the epilogue) in every precision; the forward operator (A on the loaded
@@ -155,6 +162,7 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
   if (L.mode == 3) L.threads = 64;
   if (L.mode == 4) L.threads = 128;
   p.TE = tile_extent(in->LsE, L, p.mob != 0);
+  p.brick = brick_extent(g->lat, L);
   const int64_t nthreads = p.nsite * (p.LsE / L.spt);
   const int64_t blocks = staged ? (p.nsite + NS - 1) / NS : (nthreads + L.threads - 1) / L.threads;
   Reduce red;

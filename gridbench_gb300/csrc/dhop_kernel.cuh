@@ -479,6 +479,8 @@ struct DhopParams {
   double mb = 1.0, mc = 0.0;
   // direct forms: slices per tile when each site's slices are cut into tiles (0: one tile)
   int TE = 0;
+  // direct forms on periodic lattices: sweep in t-bricks of this many t-slices (0/1: natural order)
+  int brick = 0;
 };
 
 // Writes N slices of v[N][12] (slices e0.., norms for F16); returns the sum of squares of
@@ -764,6 +766,23 @@ __global__ void __launch_bounds__(MINB > 0 ? MAXT : 256, MINB > 0 ? MINB : 1) k_
         site = r / GT;
         s0 = int(tile) * p.TE + int(r - site * GT) * N;
       }
+      if (p.brick > 1) {
+        // t-bricks: the sweep visits sites (t brick, z, y, x, t inside the brick), so a site's
+        // neighbours along t are read within a few sites of each other instead of a whole 3D
+        // volume apart (periodic lattice, Lt a multiple of the brick)
+        unsigned j = site;
+        const unsigned B = unsigned(p.brick);
+        const unsigned tin = j % B;
+        j /= B;
+        const unsigned Lx = unsigned(p.dims[0]), Ly = unsigned(p.dims[1]), Lz = unsigned(p.dims[2]);
+        const unsigned x = j % Lx;
+        j /= Lx;
+        const unsigned y = j % Ly;
+        j /= Ly;
+        const unsigned z = j % Lz;
+        const unsigned tb = j / Lz;
+        site = x + Lx * (y + Ly * (z + Lz * (tb * B + tin)));
+      }
     }
     if constexpr (BLK) {
       const unsigned l = threadIdx.x / G;  // 0..15 inside the block
@@ -826,6 +845,7 @@ struct DhopLaunch {
                    // 4: form 3 on 2x2x2x2 site blocks per 128-thread CTA (periodic, even extents)
   int stages = 4;  // staged kernels: depth of the leg ring
   int split = 1;   // forms 0 and 3: each site's Ls*nrhs slices cut into this many tiles
+  int brick = 1;   // forms 0 and 3 on periodic lattices: t-brick sweep order (1: natural order)
 };
 
 // Implemented per precision family in dhop_f64.cu / dhop_f32.cu / dhop_f16.cu.

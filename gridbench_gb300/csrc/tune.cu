@@ -1,8 +1,9 @@
 // Autotuner for the hopping kernel: times every admissible launch shape (threads per CTA,
-// slices per thread, form, ring stages, and for the direct forms the Ls / RHS tile split) on the
-// caller's own fields with CUDA events and keeps the fastest, keyed by (gauge precision, spinor
-// precision, innermost extent Ls*nrhs, epilogue).  The cache can be written to and read back from
-// a small JSON object {"key": [threads, slices, form, stages, split], ...}.
+// slices per thread, form, ring stages, and for the direct forms the Ls / RHS tile split and the
+// t-brick sweep order) on the caller's own fields with CUDA events and keeps the fastest, keyed by
+// (gauge precision, spinor precision, innermost extent Ls*nrhs, epilogue).  The cache can be
+// written to and read back from a small JSON object {"key": [threads, slices, form, stages,
+// split, brick], ...}.
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -72,6 +73,12 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
         DhopLaunch L{th, spt, 0, 4, split};
         if (split == 1 || tile_extent(in->LsE, L, false) > 0) cands.push_back(L);
       }
+      // t-brick sweep orders (periodic lattices): the other way to shorten the reuse distance,
+      // without re-reading links
+      for (int brick : {2, 4, 8}) {
+        DhopLaunch L{th, spt, 0, 4, 1, brick};
+        if (brick_extent(g->lat, L) > 0) cands.push_back(L);
+      }
     }
     for (int mode : {1, 2})
       for (int spt : {s1, s2})
@@ -86,6 +93,10 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
     for (int split : {1, 2, 3, 4, 6, 8, 12, 16}) {
       const DhopLaunch L{64, 2, 3, 4, split};
       if (split == 1 || tile_extent(in->LsE, L, false) > 0) cands.push_back(L);
+    }
+    for (int brick : {2, 4, 8}) {
+      const DhopLaunch L{64, 2, 3, 4, 1, brick};
+      if (brick_extent(g->lat, L) > 0) cands.push_back(L);
     }
   }
   if (blocked_ok(g->lat, in)) cands.push_back(DhopLaunch{128, 2, 4, 4});
@@ -184,6 +195,26 @@ int gbdw_tune_set_split(const gbdw_gauge* g, const gbdw_field* in, int split) {
   return GBDW_OK;
 }
 
+int gbdw_tune_brick(const gbdw_gauge* g, const gbdw_field* in, int* brick) {
+  if (!g || !in || !brick) return GBDW_ERR_INVALID;
+  *brick = tuned_launch(g->prec, in->prec, in->LsE, 0).brick;
+  return GBDW_OK;
+}
+
+int gbdw_tune_set_brick(const gbdw_gauge* g, const gbdw_field* in, int brick) {
+  if (!g || !in) return GBDW_ERR_INVALID;
+  DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, 0);
+  L.brick = brick;
+  if (brick < 1 || (brick > 1 && brick_extent(g->lat, L) == 0)) {
+    set_error("gbdw_tune_set_brick: the chosen form must be direct (0 or 3) on a periodic lattice whose Lt the "
+              "brick divides");
+    return GBDW_ERR_INVALID;
+  }
+  set_tuned_launch(g->prec, in->prec, in->LsE, 0, L);
+  if (in->nrhs == 1) set_tuned_launch(g->prec, in->prec, in->LsE, 1, L);
+  return GBDW_OK;
+}
+
 int gbdw_tune_save(const char* path) {
   if (!path) return GBDW_ERR_INVALID;
   FILE* f = fopen(path, "w");
@@ -195,8 +226,8 @@ int gbdw_tune_save(const char* path) {
   fprintf(f, "{");
   bool first = true;
   for (auto& kv : g_tuned) {
-    fprintf(f, "%s\n  \"%s\": [%d, %d, %d, %d, %d]", first ? "" : ",", kv.first.c_str(), kv.second.threads,
-            kv.second.spt, kv.second.mode, kv.second.stages, kv.second.split);
+    fprintf(f, "%s\n  \"%s\": [%d, %d, %d, %d, %d, %d]", first ? "" : ",", kv.first.c_str(), kv.second.threads,
+            kv.second.spt, kv.second.mode, kv.second.stages, kv.second.split, kv.second.brick);
     first = false;
   }
   fprintf(f, "\n}\n");
@@ -216,22 +247,22 @@ int gbdw_tune_load(const char* path) {
   size_t n;
   while ((n = fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, n);
   fclose(f);
-  // Entries look like "g1_s1_L16_e0": [128, 2, 0, 4, 1] (threads, slices per thread, form, stages,
-  // tile split; shorter entries keep the defaults of the missing numbers)
+  // Entries look like "g1_s1_L16_e0": [128, 2, 0, 4, 1, 1] (threads, slices per thread, form,
+  // stages, tile split, t-brick; shorter entries keep the defaults of the missing numbers)
   size_t pos = 0;
   int loaded = 0;
   while ((pos = text.find('"', pos)) != std::string::npos) {
     const size_t end = text.find('"', pos + 1);
     if (end == std::string::npos) break;
     const std::string key = text.substr(pos + 1, end - pos - 1);
-    int gp, sp, LsE, epi, th, spt, mode = 0, stages = 4, split = 1;
+    int gp, sp, LsE, epi, th, spt, mode = 0, stages = 4, split = 1, brick = 1;
     const size_t lb = text.find('[', end);
     if (lb == std::string::npos) break;
     if (sscanf(key.c_str(), "g%d_s%d_L%d_e%d", &gp, &sp, &LsE, &epi) == 4 &&
-        sscanf(text.c_str() + lb, "[%d , %d , %d , %d , %d]", &th, &spt, &mode, &stages, &split) >= 2 && th > 0 &&
-        th <= 256 && th % 32 == 0 && (spt == 1 || spt == 2 || spt == 4) && mode >= 0 && mode <= 4 &&
-        (stages == 2 || stages == 4) && split >= 1 && split <= 64) {
-      set_tuned_launch(gp, sp, LsE, epi, DhopLaunch{th, spt, mode, stages, split});
+        sscanf(text.c_str() + lb, "[%d , %d , %d , %d , %d , %d]", &th, &spt, &mode, &stages, &split, &brick) >= 2 &&
+        th > 0 && th <= 256 && th % 32 == 0 && (spt == 1 || spt == 2 || spt == 4) && mode >= 0 && mode <= 4 &&
+        (stages == 2 || stages == 4) && split >= 1 && split <= 64 && brick >= 1 && brick <= 64) {
+      set_tuned_launch(gp, sp, LsE, epi, DhopLaunch{th, spt, mode, stages, split, brick});
       ++loaded;
     }
     pos = text.find(']', lb);

@@ -39,6 +39,8 @@ bool blocked_ok(const gbdw_lattice* lat, const gbdw_field* in);
 // slices per tile of a direct launch with L.split tiles per site, or 0 (one tile: the split does
 // not divide the extent into whole slice groups, a staged or blocked form, or whole_sites)
 int tile_extent(int LsE, const DhopLaunch& L, bool whole_sites);
+// t-brick of a direct launch on a periodic lattice whose Lt it divides, or 0 (natural order)
+int brick_extent(const gbdw_lattice* lat, const DhopLaunch& L);
 // the Mobius operator (dag 0) or its adjoint (dag 1) can be fused into the hopping pass for these
 // operands (DhopExtra::mobius)
 bool mobius_fusable(const gbdw_gauge* g, const gbdw_field* in, int dag);

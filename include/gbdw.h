@@ -367,6 +367,13 @@ int gbdw_tune_set(const gbdw_gauge* g, const gbdw_field* in, int threads, int sp
  * sites; gbdw_tune_set resets it to 1). */
 int gbdw_tune_split(const gbdw_gauge* g, const gbdw_field* in, int* split);
 int gbdw_tune_set_split(const gbdw_gauge* g, const gbdw_field* in, int split);
+/* t-brick sweep order of the direct forms on periodic lattices: sites are visited as (t brick,
+ * z, y, x, t inside the brick), so neighbours along t are read close together in the sweep instead
+ * of a whole 3D volume apart (what lets a site's spinor leave L2 before its next reader when a
+ * site holds many slices, e.g. many right-hand sides).  The tuner chooses among 1 (natural order),
+ * 2, 4, 8; gbdw_tune_brick reads the choice, gbdw_tune_set_brick pins it (Lt must be a multiple). */
+int gbdw_tune_brick(const gbdw_gauge* g, const gbdw_field* in, int* brick);
+int gbdw_tune_set_brick(const gbdw_gauge* g, const gbdw_field* in, int brick);
 
 /* ------------------------------------------------------------------ timing on the library stream */
 typedef struct gbdw_timer gbdw_timer;

@@ -398,3 +398,58 @@ def test_multi_rhs_tile_sweeps(gpu, form, threads, split):
             ref = oracle.dslash(c["U"], srcs[r], c["nbr"], c["prm"], c["nsite"], Ls, dag)
             assert rel_err(Y.numpy(r), ref) < TOL[gb.F32], (form, split, dag, r)
     gb.synchronize()
+
+
+@pytest.mark.parametrize("form,threads", [(0, 128), (3, 64)])
+@pytest.mark.parametrize("brick", [2, 4, 8])
+def test_t_brick_sweep_orders(gpu, form, threads, brick):
+    """t-brick sweep orders of the direct forms on a periodic lattice (Lt = 8): Dhop, DhopDag and
+    M at Ls = 16, 12 right-hand sides at Ls = 12 (form 3 at Ls*nrhs = 144), the Mobius adjoint's
+    single pass, and a brick combined with a tile split — all against the oracle."""
+    from oracle import mobius as mob
+    dims = (4, 2, 4, 8)
+    c = make_case(dims, 16)
+    lat = gb.Lattice.periodic(dims, 16)
+    g = gb.Gauge(lat, c["U"], gb.F32)
+    x, y, t = gb.Field(lat, gb.F32).load(c["phi"]), gb.Field(lat, gb.F32), gb.Field(lat, gb.F32)
+    gb.tune_set(g, x, threads, 2, form, 4)
+    gb.tune_set_brick(g, x, brick)
+    assert gb.tune_brick(g, x) == brick
+    for dag in (0, 1):
+        y.zero()
+        gb.dhop(g, y, x, dag)
+        assert rel_err(y.numpy(), oracle.dslash(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], 16, dag)) < 1e-6
+        n2 = gb.dwf_m(g, y, x, 1.8, 0.01, dag, want_norm=True)
+        out = y.numpy()
+        assert rel_err(out, oracle.dwf_m(c["U"], c["phi"], c["nbr"], c["nsite"], 16, 1.8, 0.01, dag)) < 1e-6
+        assert abs(n2 - float(np.sum(out ** 2))) / n2 < 1e-5
+        gb.mobius_m(g, y, t, x, 1.5, 0.5, 1.8, 0.01, dag)
+        ref = mob.mobius_m(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], 16, 1.5, 0.5, 1.8, 0.01, dag)
+        assert rel_err(y.numpy(), ref) < 1e-6, dag
+    if form == 0:
+        gb.tune_set_split(g, x, 2)  # a brick and a tile split together
+        gb.dhop(g, y, x)
+        assert rel_err(y.numpy(), oracle.dslash(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], 16)) < 1e-6
+    Ls, k = 12, 12
+    c = make_case(dims, Ls)
+    lat = gb.Lattice.periodic(dims, Ls)
+    g = gb.Gauge(lat, c["U"], gb.F32)
+    X, Y = gb.Field(lat, gb.F32, k), gb.Field(lat, gb.F32, k)
+    srcs = [gb.generate_fermion(dims, Ls, 1, (5 + r, 6, 7, 8)) for r in range(k)]
+    for r in range(k):
+        X.load(srcs[r], r)
+    gb.tune_set(g, X, threads, 2, form, 4)
+    gb.tune_set_brick(g, X, brick)
+    gb.dhop(g, Y, X)
+    for r in range(k):
+        ref = oracle.dslash(c["U"], srcs[r], c["nbr"], c["prm"], c["nsite"], Ls)
+        assert rel_err(Y.numpy(r), ref) < 1e-6, r
+    with pytest.raises(gb.GbdwError):
+        gb.tune_set_brick(g, X, 3)  # Lt = 8 is not a multiple of 3
+    lt = gb.Lattice.from_table(c["nbr"], c["prm"], c["nsite"], Ls)  # no extents: no bricks
+    gt = gb.Gauge(lt, c["U"], gb.F32)
+    xt = gb.Field(lt, gb.F32, k)
+    gb.tune_set(gt, xt, threads, 2, form, 4)
+    with pytest.raises(gb.GbdwError):
+        gb.tune_set_brick(gt, xt, 2)
+    gb.synchronize()
