@@ -466,7 +466,8 @@ def bench_mrhs(gb, peak) -> dict:
             "byte_model_ceiling": round(algo_bytes(1, 1, Ls, 1) / algo_bytes(1, 1, Ls, k), 3),
             "hbm_frac_12rhs": round(algo_bytes(1, 1, Ls, k) * V5 * k / t_multi / 1e9 / peak, 3),
             "rel_err_vs_single": err, "rel_err_vs_fp64": err64, "launch": list(gb.tune_query(g, X)),
-            "tile_split": gb.tune_split(g, X)}
+            "tile_split": gb.tune_split(g, X), "t_brick": gb.tune_brick(g, X),
+            "single_rhs_launch": list(gb.tune_query(g, x1)) + [gb.tune_split(g, x1), gb.tune_brick(g, x1)]}
 
 
 def bench_batch(gb, peak, nrhs_choices=(1,), seed=2024, vols=(8, 12, 16, 20, 24)) -> dict:
@@ -715,7 +716,7 @@ def run_ours(args, D: Dist) -> dict | None:
         "launch": {"threads": cfg[0], "slices_per_thread": cfg[1],
                    "form": {0: "direct", 1: "tma-staged (CTA ring)", 2: "tma-staged (warp rings)",
                             3: "direct (Ls=16 specialised)", 4: "direct (Ls=16, 2^4 site blocks)"}[cfg[2]],
-                   "stages": cfg[3], "tile_split": gb.tune_split(g, xA)},
+                   "stages": cfg[3], "tile_split": gb.tune_split(g, xA), "t_brick": gb.tune_brick(g, xA)},
         "rel_err_vs_fp64": rel,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,

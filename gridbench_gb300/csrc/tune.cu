@@ -94,10 +94,13 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
       const DhopLaunch L{64, 2, 3, 4, split};
       if (split == 1 || tile_extent(in->LsE, L, false) > 0) cands.push_back(L);
     }
-    for (int brick : {2, 4, 8}) {
-      const DhopLaunch L{64, 2, 3, 4, 1, brick};
-      if (brick_extent(g->lat, L) > 0) cands.push_back(L);
-    }
+    // t-bricks alone and with tile splits (measured at 24^4 x 12 with 12 right-hand sides: bricks
+    // of 4 t-slices swept in 3 tiles beat either alone)
+    for (int brick : {2, 4, 8})
+      for (int split : {1, 2, 3, 4, 6}) {
+        const DhopLaunch L{64, 2, 3, 4, split, brick};
+        if (brick_extent(g->lat, L) > 0 && (split == 1 || tile_extent(in->LsE, L, false) > 0)) cands.push_back(L);
+      }
   }
   if (blocked_ok(g->lat, in)) cands.push_back(DhopLaunch{128, 2, 4, 4});
   cudaEvent_t a, b;
