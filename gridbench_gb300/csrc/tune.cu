@@ -107,31 +107,51 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
   GBDW_CUDA(cudaEventCreate(&a));
   GBDW_CUDA(cudaEventCreate(&b));
   const DhopLaunch saved = tuned_launch(g->prec, in->prec, in->LsE, 0);
-  DhopLaunch best = saved;
-  float best_ms = 1e30f;
+  DhopLaunch best = saved, best_nat = saved;
+  float best_ms = 1e30f, best_nat_ms = 1e30f;
   int status = GBDW_OK;
-  for (const DhopLaunch& L : cands) {
-    set_tuned_launch(g->prec, in->prec, in->LsE, 0, L);
-    for (int w = 0; w < 3 && !status; ++w) status = run_dhop(g, out, in, dag, 0, 0.0, 0.0, nullptr);
-    if (status) break;
+  // time reps launches of the hopping term (epi 0) or of M (epi 1) with shape L
+  auto time_shape = [&](const DhopLaunch& L, int epi, float* ms) -> int {
+    set_tuned_launch(g->prec, in->prec, in->LsE, epi, L);
+    int st = GBDW_OK;
+    for (int w = 0; w < 3 && !st; ++w) st = run_dhop(g, out, in, dag, epi, 1.2, 0.01, nullptr);
+    if (st) return st;
     const int reps = 10;
     cudaEventRecord(a, stream());
-    for (int r = 0; r < reps && !status; ++r) status = run_dhop(g, out, in, dag, 0, 0.0, 0.0, nullptr);
+    for (int r = 0; r < reps && !st; ++r) st = run_dhop(g, out, in, dag, epi, 1.2, 0.01, nullptr);
     cudaEventRecord(b, stream());
     cudaEventSynchronize(b);
-    if (status) break;
+    if (st) return st;
+    cudaEventElapsedTime(ms, a, b);
+    return GBDW_OK;
+  };
+  for (const DhopLaunch& L : cands) {
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, a, b);
+    if ((status = time_shape(L, 0, &ms))) break;
     if (ms < best_ms) {
       best_ms = ms;
       best = L;
     }
+    if (L.split == 1 && L.brick == 1 && ms < best_nat_ms) {
+      best_nat_ms = ms;
+      best_nat = L;
+    }
+  }
+  set_tuned_launch(g->prec, in->prec, in->LsE, 0, status ? saved : best);
+  if (!status && in->nrhs == 1) {
+    // M (the Shamir epilogue reads the centre site and its 5th-dimension neighbours, and the CG
+    // passes take this shape with their residual epilogues): the Dhop choice if it sweeps in
+    // the natural order, else whichever of it and the best natural-order shape M runs faster with
+    DhopLaunch m = best;
+    if (best.split != 1 || best.brick != 1) {
+      float m_best = 0.f, m_nat = 0.f;
+      if (!(status = time_shape(best, 1, &m_best)) && !(status = time_shape(best_nat, 1, &m_nat)))
+        m = m_nat <= m_best ? best_nat : best;
+    }
+    set_tuned_launch(g->prec, in->prec, in->LsE, 1, status ? best_nat : m);
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
-  set_tuned_launch(g->prec, in->prec, in->LsE, 0, status ? saved : best);
-  // The M epilogue reads the centre site as well; reuse the choice for it.
-  if (!status && in->nrhs == 1) set_tuned_launch(g->prec, in->prec, in->LsE, 1, best);
   return status;
 }
 
