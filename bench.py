@@ -564,9 +564,12 @@ def bench_cg(gb, args) -> dict:
     g64 = gb.Gauge(lat, None, gb.F64, seed=77)
     g32 = gb.Gauge(lat, None, gb.F32, seed=77)
     g16 = gb.Gauge(lat, None, gb.F16, seed=77)
-    for g, sp in ((g32, gb.F32), (g16, gb.F16)):
+    m_shapes = {}
+    for g, sp, tag in ((g32, gb.F32, "fp32"), (g16, gb.F16, "fp16")):
         x, y = gb.Field(lat, sp).gaussian(1), gb.Field(lat, sp)
         gb.tune_dhop(g, y, x)
+        m_shapes[tag] = {"dhop": list(gb.tune_query(g, x)) + [gb.tune_split(g, x), gb.tune_brick(g, x)],
+                         "m_and_cg_passes": list(gb.tune_query_m(g, x))}
         del x, y
     G64 = (g64.checkerboard(le), g64.checkerboard(lo))
     G32 = (g32.checkerboard(le), g32.checkerboard(lo))
@@ -575,7 +578,8 @@ def bench_cg(gb, args) -> dict:
     res = {"lattice": f"{'x'.join(map(str, dims))} x Ls={Ls}", "M5": M5, "mf": mf, "tol": 1e-10,
            "full": "CG on M^dag M x = b; true_residual = |b - M^dag M x| / |b|",
            "eo": "M x = b by CG on the odd Schur normal system (tol on its true residual); "
-                 "true_residual = |b - M x| / |b| after reconstruction"}
+                 "true_residual = |b - M x| / |b| after reconstruction",
+           "launch": m_shapes, "launch_fields": "threads, slices/thread, form, stages, tile split, t-brick"}
     it = args.cg_max_iter
     runs = (
         ("full_plain_fp32_fp64res", 1e-4, lambda x, d: gb.cg_solve(g64, x, b, M5, mf, gb.CG_PLAIN, max_iter=it, delta=d,

@@ -513,6 +513,14 @@ def tune_set_brick(g: Gauge, inp: Field, brick: int):
     check(load().gbdw_tune_set_brick(g.h, inp.h, int(brick)))
 
 
+def tune_query_m(g: Gauge, inp: Field) -> tuple:
+    """(threads, slices per thread, form, stages, split, brick) of the Shamir M pass and the CG
+    passes built on it, for fields like inp with one right-hand side."""
+    cfg = (C.c_int * 6)()
+    check(load().gbdw_tune_query_m(g.h, inp.h, cfg))
+    return tuple(int(v) for v in cfg)
+
+
 def tune_save(path: str):
     check(load().gbdw_tune_save(path.encode()))
 

@@ -107,8 +107,8 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
   GBDW_CUDA(cudaEventCreate(&a));
   GBDW_CUDA(cudaEventCreate(&b));
   const DhopLaunch saved = tuned_launch(g->prec, in->prec, in->LsE, 0);
-  DhopLaunch best = saved, best_nat = saved;
-  float best_ms = 1e30f, best_nat_ms = 1e30f;
+  DhopLaunch best = saved, best_m = saved;
+  float best_ms = 1e30f, best_m_ms = 1e30f;
   int status = GBDW_OK;
   // time reps launches of the hopping term (epi 0) or of M (epi 1) with shape L
   auto time_shape = [&](const DhopLaunch& L, int epi, float* ms) -> int {
@@ -125,6 +125,11 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
     cudaEventElapsedTime(ms, a, b);
     return GBDW_OK;
   };
+  // M (one right-hand side) is timed over the same shapes on its own: its epilogue reads the
+  // centre site's 5th-dimension neighbours, and the CG passes run on its shape with their
+  // residual epilogues.  Measured at 32^4 x 16: the hopping term's best sweep (form 3 in t-bricks
+  // of 8) cost the FP32 CG 7 % against the staged form that M alone prefers.
+  const DhopLaunch saved_m = tuned_launch(g->prec, in->prec, in->LsE, 1);
   for (const DhopLaunch& L : cands) {
     float ms = 0.f;
     if ((status = time_shape(L, 0, &ms))) break;
@@ -132,24 +137,15 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
       best_ms = ms;
       best = L;
     }
-    if (L.split == 1 && L.brick == 1 && ms < best_nat_ms) {
-      best_nat_ms = ms;
-      best_nat = L;
+    if (in->nrhs != 1) continue;
+    if ((status = time_shape(L, 1, &ms))) break;
+    if (ms < best_m_ms) {
+      best_m_ms = ms;
+      best_m = L;
     }
   }
   set_tuned_launch(g->prec, in->prec, in->LsE, 0, status ? saved : best);
-  if (!status && in->nrhs == 1) {
-    // M (the Shamir epilogue reads the centre site and its 5th-dimension neighbours, and the CG
-    // passes take this shape with their residual epilogues): the Dhop choice if it sweeps in
-    // the natural order, else whichever of it and the best natural-order shape M runs faster with
-    DhopLaunch m = best;
-    if (best.split != 1 || best.brick != 1) {
-      float m_best = 0.f, m_nat = 0.f;
-      if (!(status = time_shape(best, 1, &m_best)) && !(status = time_shape(best_nat, 1, &m_nat)))
-        m = m_nat <= m_best ? best_nat : best;
-    }
-    set_tuned_launch(g->prec, in->prec, in->LsE, 1, status ? best_nat : m);
-  }
+  if (in->nrhs == 1) set_tuned_launch(g->prec, in->prec, in->LsE, 1, status ? saved_m : best_m);
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   return status;
@@ -162,6 +158,14 @@ int gbdw_tune_query(const gbdw_gauge* g, const gbdw_field* in, int cfg[4]) {
   cfg[1] = L.spt;
   cfg[2] = L.mode;
   cfg[3] = L.stages;
+  return GBDW_OK;
+}
+
+int gbdw_tune_query_m(const gbdw_gauge* g, const gbdw_field* in, int cfg[6]) {
+  if (!g || !in || !cfg) return GBDW_ERR_INVALID;
+  const DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, 1);
+  const int v[6] = {L.threads, L.spt, L.mode, L.stages, L.split, L.brick};
+  for (int i = 0; i < 6; ++i) cfg[i] = v[i];
   return GBDW_OK;
 }
 

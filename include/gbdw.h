@@ -374,6 +374,11 @@ int gbdw_tune_set_split(const gbdw_gauge* g, const gbdw_field* in, int split);
  * 2, 4, 8; gbdw_tune_brick reads the choice, gbdw_tune_set_brick pins it (Lt must be a multiple). */
 int gbdw_tune_brick(const gbdw_gauge* g, const gbdw_field* in, int* brick);
 int gbdw_tune_set_brick(const gbdw_gauge* g, const gbdw_field* in, int brick);
+/* The shape of the Shamir M pass (and of the CG passes built on it) for fields like `in` with one
+ * right-hand side: cfg[6] = threads, slices per thread, form, stages, split, brick.  gbdw_tune_dhop
+ * times M over the same candidates as the hopping term and keeps its own fastest; the gbdw_tune_set*
+ * calls pin both. */
+int gbdw_tune_query_m(const gbdw_gauge* g, const gbdw_field* in, int cfg[6]);
 
 /* ------------------------------------------------------------------ timing on the library stream */
 typedef struct gbdw_timer gbdw_timer;

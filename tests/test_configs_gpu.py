@@ -62,6 +62,26 @@ def test_fp32_16x16_matches_oracle_in_every_form(headline, dag):
         assert rel_err(y.numpy(), refs[dag]) <= TOL[gb.F32], shape
 
 
+@pytest.mark.parametrize("dag", [0, 1])
+def test_fp32_16x16_m_on_its_own_tuned_shape(headline, dag):
+    """M (the CG's operator) runs on the shape the tuner timed for M itself, which may differ
+    from the hopping term's; both match the oracle, and gbdw_tune_set pins the two together."""
+    c, lat, _ = headline
+    g = gb.Gauge(lat, c["U"], gb.F32)
+    x, y = gb.Field(lat, gb.F32).load(c["phi"]), gb.Field(lat, gb.F32)
+    gb.tune_dhop(g, y, x, dag)
+    m_shape = gb.tune_query_m(g, x)
+    assert len(m_shape) == 6 and m_shape[2] in range(5) and m_shape[4] >= 1 and m_shape[5] >= 1
+    ref = oracle.dwf_m(c["U"], c["phi"], c["nbr"], c["nsite"], 16, 1.8, 0.01, dag)
+    gb.dwf_m(g, y, x, 1.8, 0.01, dag)
+    assert rel_err(y.numpy(), ref) <= TOL[gb.F32]
+    gb.tune_set(g, x, 64, 2, 2, 2)
+    assert gb.tune_query_m(g, x) == (64, 2, 2, 2, 1, 1)
+    y.zero()
+    gb.dwf_m(g, y, x, 1.8, 0.01, dag)
+    assert rel_err(y.numpy(), ref) <= TOL[gb.F32]
+
+
 def test_fp16_16x16_matches_oracle(headline):
     """The mixed CG's sloppy operator (FP16 spinors with per-slice norms, 12-real FP16 links)
     at the headline shape, with the tuner's pick."""
