@@ -569,7 +569,10 @@ def bench_cg(gb, args) -> dict:
         x, y = gb.Field(lat, sp).gaussian(1), gb.Field(lat, sp)
         gb.tune_dhop(g, y, x)
         m_shapes[tag] = {"dhop": list(gb.tune_query(g, x)) + [gb.tune_split(g, x), gb.tune_brick(g, x)],
-                         "m_and_cg_passes": list(gb.tune_query_m(g, x))}
+                         "m": list(gb.tune_query_m(g, x)),
+                         "cg_step_r_fp64" if sp == gb.F32 else "cg_step_r_fp16":
+                             list(gb.tune_query_cg(g, x, gb.F64 if sp == gb.F32 else gb.F16)),
+                         "cg_step_r_fp32": list(gb.tune_query_cg(g, x, gb.F32))}
         del x, y
     G64 = (g64.checkerboard(le), g64.checkerboard(lo))
     G32 = (g32.checkerboard(le), g32.checkerboard(lo))

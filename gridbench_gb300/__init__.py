@@ -521,6 +521,14 @@ def tune_query_m(g: Gauge, inp: Field) -> tuple:
     return tuple(int(v) for v in cfg)
 
 
+def tune_query_cg(g: Gauge, inp: Field, rprec: int) -> tuple:
+    """The same six numbers for the fused CG step (M^dag M with the residual update) with an
+    iterated residual of precision rprec (F64, F32 or F16)."""
+    cfg = (C.c_int * 6)()
+    check(load().gbdw_tune_query_cg(g.h, inp.h, int(rprec), cfg))
+    return tuple(int(v) for v in cfg)
+
+
 def tune_save(path: str):
     check(load().gbdw_tune_save(path.encode()))
 

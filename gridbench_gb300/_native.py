@@ -126,6 +126,7 @@ PROTOTYPES = {
     "gbdw_tune_brick": (_i, [_vp, _vp, C.POINTER(C.c_int)]),
     "gbdw_tune_set_brick": (_i, [_vp, _vp, _i]),
     "gbdw_tune_query_m": (_i, [_vp, _vp, C.POINTER(C.c_int)]),
+    "gbdw_tune_query_cg": (_i, [_vp, _vp, _i, C.POINTER(C.c_int)]),
     "gbdw_selftest_wait_timeout": (_i, [_u64]),
     "gbdw_timer_create": (_i, [_pp]),
     "gbdw_timer_start": (_i, [_vp]),

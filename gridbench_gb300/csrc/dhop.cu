@@ -150,6 +150,7 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
     return GBDW_ERR_ALLOC;
   }
   DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, tune_epi);
+  if (ex && ex->tune_key >= 0) find_tuned_launch(g->prec, in->prec, in->LsE, ex->tune_key, &L);
   if (in->LsE % L.spt != 0) L.spt = 1;
   if (p.mob) L.spt = 2;  // the fused adjoint works on slice pairs, one site's pairs in consecutive lanes
   int NS = 0, tthreads = 0;
@@ -231,11 +232,13 @@ int mdagm_residual(const gbdw_gauge* g, gbdw_field* t, gbdw_field* r, const gbdw
   e1.sum_to = s;
   e1.num = rr;
   e1.alpha_to = s + 1;
+  e1.tune_key = cg_step_key(r->prec);
   if (int st = run_dhop(g, t, p, 0, 1, 5.0 - M5, mf, nullptr, false, nullptr, 0.5, &e1)) return st;
   DhopExtra e2;
   e2.r = r;
   e2.alpha = s + 1;
   e2.sum_to = s + 2;
+  e2.tune_key = e1.tune_key;
   if (int st = run_dhop(g, t, t, 1, 1, 5.0 - M5, mf, nullptr, false, nullptr, 0.5, &e2)) return st;
   return fetch_doubles(s, 3, out);
 }

@@ -4,6 +4,7 @@
 // (gauge precision, spinor precision, innermost extent Ls*nrhs, epilogue).  The cache can be
 // written to and read back from a small JSON object {"key": [threads, slices, form, stages,
 // split, brick], ...}.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -43,9 +44,38 @@ DhopLaunch tuned_launch(int gprec, int sprec, int LsE, int epi) {
   return default_launch(gprec, sprec, LsE, epi);
 }
 
+bool find_tuned_launch(int gprec, int sprec, int LsE, int epi, DhopLaunch* L) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tuned.find(key_of(gprec, sprec, LsE, epi));
+  if (it == g_tuned.end()) return false;
+  *L = it->second;
+  return true;
+}
+
 void set_tuned_launch(int gprec, int sprec, int LsE, int epi, DhopLaunch L) {
   std::lock_guard<std::mutex> lk(g_tune_mu);
   g_tuned[key_of(gprec, sprec, LsE, epi)] = L;
+}
+
+// residual precisions of the fused CG step for an operator on spinors of precision sprec
+// (mdagm_residual: FP64 or FP32 r with an FP32 operator, FP32 or, with FP16 links, FP16 r with FP16)
+std::vector<int> cg_residual_precs(int gprec, int sprec) {
+  if (sprec == GBDW_F32) return {GBDW_F64, GBDW_F32};
+  if (sprec == GBDW_F16) return gprec == GBDW_F16 ? std::vector<int>{GBDW_F32, GBDW_F16} : std::vector<int>{GBDW_F32};
+  return {};
+}
+
+// a pinned shape applies to the hopping term and, with one right-hand side, to M and the CG steps
+void pin_launch(const gbdw_gauge* g, const gbdw_field* in, const DhopLaunch& L) {
+  set_tuned_launch(g->prec, in->prec, in->LsE, 0, L);
+  if (in->nrhs != 1) return;
+  set_tuned_launch(g->prec, in->prec, in->LsE, 1, L);
+  for (int rp : cg_residual_precs(g->prec, in->prec)) set_tuned_launch(g->prec, in->prec, in->LsE, cg_step_key(rp), L);
+}
+
+bool same_launch(const DhopLaunch& a, const DhopLaunch& b) {
+  return a.threads == b.threads && a.spt == b.spt && a.mode == b.mode && a.stages == b.stages && a.split == b.split &&
+         a.brick == b.brick;
 }
 
 }  // namespace gbdw
@@ -130,6 +160,7 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
   // residual epilogues.  Measured at 32^4 x 16: the hopping term's best sweep (form 3 in t-bricks
   // of 8) cost the FP32 CG 7 % against the staged form that M alone prefers.
   const DhopLaunch saved_m = tuned_launch(g->prec, in->prec, in->LsE, 1);
+  std::vector<std::pair<float, DhopLaunch>> m_times;
   for (const DhopLaunch& L : cands) {
     float ms = 0.f;
     if ((status = time_shape(L, 0, &ms))) break;
@@ -139,6 +170,7 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
     }
     if (in->nrhs != 1) continue;
     if ((status = time_shape(L, 1, &ms))) break;
+    m_times.push_back({ms, L});
     if (ms < best_m_ms) {
       best_m_ms = ms;
       best_m = L;
@@ -146,6 +178,58 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
   }
   set_tuned_launch(g->prec, in->prec, in->LsE, 0, status ? saved : best);
   if (in->nrhs == 1) set_tuned_launch(g->prec, in->prec, in->LsE, 1, status ? saved_m : best_m);
+  // The fused CG step (mdagm_residual: M with |Mp|^2 and alpha reduced, then M^dag with r updated
+  // and |r|^2 reduced) reads and writes r besides M's traffic, so its best shape can differ from
+  // M's (measured at 32^4 x 16 with an FP64 r: M alone fastest in t-bricks of 8 on form 3, the CG
+  // step 7 % faster on the staged form).  It is timed on the real pass over a shortlist: M's four
+  // fastest shapes and the fastest natural-order shape of each form.
+  if (!status && in->nrhs == 1 && !m_times.empty()) {
+    std::stable_sort(m_times.begin(), m_times.end(),
+                     [](const std::pair<float, DhopLaunch>& x, const std::pair<float, DhopLaunch>& y) {
+                       return x.first < y.first;
+                     });
+    std::vector<DhopLaunch> shortlist;
+    auto add = [&](const DhopLaunch& L) {
+      for (const DhopLaunch& q : shortlist)
+        if (same_launch(q, L)) return;
+      shortlist.push_back(L);
+    };
+    for (size_t i = 0; i < m_times.size() && i < 4; ++i) add(m_times[i].second);
+    for (int form = 0; form <= 4; ++form)
+      for (const auto& mt : m_times)
+        if (mt.second.mode == form && mt.second.split == 1 && mt.second.brick == 1) {
+          add(mt.second);
+          break;
+        }
+    for (int rp : cg_residual_precs(g->prec, in->prec)) {
+      gbdw_field* r = nullptr;
+      if ((status = gbdw_field_create(&r, in->lat, rp, 1))) break;
+      const int key = cg_step_key(rp);
+      DhopLaunch best_cg = best_m;
+      float best_cg_ms = 1e30f;
+      for (const DhopLaunch& L : shortlist) {
+        set_tuned_launch(g->prec, in->prec, in->LsE, key, L);
+        double o3[3];
+        for (int w = 0; w < 2 && !status; ++w) status = mdagm_residual(g, out, r, in, 1.8, 0.01, 1.0, o3);
+        if (status) break;
+        const int reps = 6;
+        cudaEventRecord(a, stream());
+        for (int k = 0; k < reps && !status; ++k) status = mdagm_residual(g, out, r, in, 1.8, 0.01, 1.0, o3);
+        cudaEventRecord(b, stream());
+        cudaEventSynchronize(b);
+        if (status) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        if (ms < best_cg_ms) {
+          best_cg_ms = ms;
+          best_cg = L;
+        }
+      }
+      set_tuned_launch(g->prec, in->prec, in->LsE, key, status ? best_m : best_cg);
+      gbdw_field_destroy(r);
+      if (status) break;
+    }
+  }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   return status;
@@ -164,6 +248,15 @@ int gbdw_tune_query(const gbdw_gauge* g, const gbdw_field* in, int cfg[4]) {
 int gbdw_tune_query_m(const gbdw_gauge* g, const gbdw_field* in, int cfg[6]) {
   if (!g || !in || !cfg) return GBDW_ERR_INVALID;
   const DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, 1);
+  const int v[6] = {L.threads, L.spt, L.mode, L.stages, L.split, L.brick};
+  for (int i = 0; i < 6; ++i) cfg[i] = v[i];
+  return GBDW_OK;
+}
+
+int gbdw_tune_query_cg(const gbdw_gauge* g, const gbdw_field* in, int rprec, int cfg[6]) {
+  if (!g || !in || !cfg || rprec < GBDW_F64 || rprec > GBDW_F16) return GBDW_ERR_INVALID;
+  DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, 1);
+  find_tuned_launch(g->prec, in->prec, in->LsE, cg_step_key(rprec), &L);
   const int v[6] = {L.threads, L.spt, L.mode, L.stages, L.split, L.brick};
   for (int i = 0; i < 6; ++i) cfg[i] = v[i];
   return GBDW_OK;
@@ -197,8 +290,7 @@ int gbdw_tune_set(const gbdw_gauge* g, const gbdw_field* in, int threads, int sp
       return GBDW_ERR_INVALID;
     }
   }
-  set_tuned_launch(g->prec, in->prec, in->LsE, 0, L);
-  if (in->nrhs == 1) set_tuned_launch(g->prec, in->prec, in->LsE, 1, L);
+  pin_launch(g, in, L);
   return GBDW_OK;
 }
 
@@ -217,8 +309,7 @@ int gbdw_tune_set_split(const gbdw_gauge* g, const gbdw_field* in, int split) {
               "slice groups");
     return GBDW_ERR_INVALID;
   }
-  set_tuned_launch(g->prec, in->prec, in->LsE, 0, L);
-  if (in->nrhs == 1) set_tuned_launch(g->prec, in->prec, in->LsE, 1, L);
+  pin_launch(g, in, L);
   return GBDW_OK;
 }
 
@@ -237,8 +328,7 @@ int gbdw_tune_set_brick(const gbdw_gauge* g, const gbdw_field* in, int brick) {
               "brick divides");
     return GBDW_ERR_INVALID;
   }
-  set_tuned_launch(g->prec, in->prec, in->LsE, 0, L);
-  if (in->nrhs == 1) set_tuned_launch(g->prec, in->prec, in->LsE, 1, L);
+  pin_launch(g, in, L);
   return GBDW_OK;
 }
 

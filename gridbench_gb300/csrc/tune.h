@@ -19,7 +19,13 @@ struct DhopExtra {
   // on DhopDag in before the epilogue (dag 1); epi 1, one right-hand side, Ls a power of two <= 64
   bool mobius = false;
   double mb = 1.0, mc = 0.0;
+  // a tune-cache key to take the launch shape from when it holds one (else the epilogue's own)
+  int tune_key = -1;
 };
+// tune-cache key of the fused CG step (both passes of mdagm_residual) with a residual of precision rprec
+inline int cg_step_key(int rprec) { return 16 + rprec; }
+// the cached shape for the key, if one was tuned or pinned
+bool find_tuned_launch(int gprec, int sprec, int LsE, int epi, DhopLaunch* L);
 // cen / khop: the M epilogue's diagonal field (default: in) and hopping coefficient (1/2)
 int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag, int epi, double a5, double mf,
              double* norm2, bool fetch = true, const gbdw_field* cen = nullptr, double khop = 0.5,

@@ -377,8 +377,12 @@ int gbdw_tune_set_brick(const gbdw_gauge* g, const gbdw_field* in, int brick);
 /* The shape of the Shamir M pass (and of the CG passes built on it) for fields like `in` with one
  * right-hand side: cfg[6] = threads, slices per thread, form, stages, split, brick.  gbdw_tune_dhop
  * times M over the same candidates as the hopping term and keeps its own fastest; the gbdw_tune_set*
- * calls pin both. */
+ * calls pin the hopping term, M and the CG steps together. */
 int gbdw_tune_query_m(const gbdw_gauge* g, const gbdw_field* in, int cfg[6]);
+/* The shape of the fused CG step (M with |M p|^2 reduced, then M^dag with r -= alpha M^dag M p and
+ * |r|^2 reduced) for an iterated residual of precision rprec (GBDW_F64/F32/F16), same cfg[6]
+ * layout.  gbdw_tune_dhop times that step on a shortlist of M's fastest shapes; untuned, it is M's. */
+int gbdw_tune_query_cg(const gbdw_gauge* g, const gbdw_field* in, int rprec, int cfg[6]);
 
 /* ------------------------------------------------------------------ timing on the library stream */
 typedef struct gbdw_timer gbdw_timer;

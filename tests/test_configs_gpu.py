@@ -75,8 +75,12 @@ def test_fp32_16x16_m_on_its_own_tuned_shape(headline, dag):
     ref = oracle.dwf_m(c["U"], c["phi"], c["nbr"], c["nsite"], 16, 1.8, 0.01, dag)
     gb.dwf_m(g, y, x, 1.8, 0.01, dag)
     assert rel_err(y.numpy(), ref) <= TOL[gb.F32]
+    for rp in (gb.F64, gb.F32):
+        cg = gb.tune_query_cg(g, x, rp)
+        assert len(cg) == 6 and cg[2] in range(5)
     gb.tune_set(g, x, 64, 2, 2, 2)
     assert gb.tune_query_m(g, x) == (64, 2, 2, 2, 1, 1)
+    assert gb.tune_query_cg(g, x, gb.F64) == (64, 2, 2, 2, 1, 1)
     y.zero()
     gb.dwf_m(g, y, x, 1.8, 0.01, dag)
     assert rel_err(y.numpy(), ref) <= TOL[gb.F32]
