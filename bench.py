@@ -577,6 +577,13 @@ def bench_cg(gb, args) -> dict:
     G64 = (g64.checkerboard(le), g64.checkerboard(lo))
     G32 = (g32.checkerboard(le), g32.checkerboard(lo))
     G16 = (g16.checkerboard(le), g16.checkerboard(lo))
+    for G, sp, tag in ((G32, gb.F32, "fp32"), (G16, gb.F16, "fp16")):
+        # the even-odd operator tunes on its own operands (gauge and output on the even half)
+        xo, ye = gb.Field(lo, sp).gaussian(1), gb.Field(le, sp)
+        gb.tune_dhop(G[0], ye, xo)
+        m_shapes[tag]["eo_hop"] = list(gb.tune_query(G[0], xo)) + [gb.tune_split(G[0], xo), 1]
+        m_shapes[tag]["eo_schur"] = list(gb.tune_query_m(G[0], xo))
+        del xo, ye
     b = gb.Field(lat, gb.F64).gaussian(78)
     res = {"lattice": f"{'x'.join(map(str, dims))} x Ls={Ls}", "M5": M5, "mf": mf, "tol": 1e-10,
            "full": "CG on M^dag M x = b; true_residual = |b - M^dag M x| / |b|",

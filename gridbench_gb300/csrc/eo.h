@@ -5,6 +5,8 @@
 namespace gbdw {
 // out = D5^-1 in (D5^-dag for dag), site-local, any lattice
 int m5inv(gbdw_field* out, const gbdw_field* in, double M5, double mf, int dag);
+// operands of the even-odd hopping term: gauge and out on one half lattice, in on its partner
+int check_eo(const gbdw_gauge* g, const gbdw_field* out, const gbdw_field* in);
 // out (half p) = Dhop_pq in (half q); with cen (half p): out = D5 cen - khop Dhop_pq in
 struct DhopExtra;
 int hop_eo(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag, const gbdw_field* cen, double M5,

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "eo.h"
 #include "tune.h"
 
 namespace gbdw {
@@ -65,11 +66,22 @@ std::vector<int> cg_residual_precs(int gprec, int sprec) {
   return {};
 }
 
+// the shape run_dhop takes for epilogue key epi with this gauge field (half lattices: their own
+// entry if one exists)
+DhopLaunch lookup(const gbdw_gauge* g, const gbdw_field* in, int epi) {
+  DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, epi);
+  if (g->lat->parity >= 0) find_tuned_launch(g->prec, in->prec, in->LsE, epi + EO_KEY, &L);
+  return L;
+}
+
 // a pinned shape applies to the hopping term and, with one right-hand side, to M and the CG steps
+// (on a half-lattice gauge field: to the even-odd hopping term and its Schur epilogue)
 void pin_launch(const gbdw_gauge* g, const gbdw_field* in, const DhopLaunch& L) {
-  set_tuned_launch(g->prec, in->prec, in->LsE, 0, L);
+  const int ko = g->lat->parity >= 0 ? EO_KEY : 0;
+  set_tuned_launch(g->prec, in->prec, in->LsE, ko, L);
   if (in->nrhs != 1) return;
-  set_tuned_launch(g->prec, in->prec, in->LsE, 1, L);
+  set_tuned_launch(g->prec, in->prec, in->LsE, 1 + ko, L);
+  if (ko) return;
   for (int rp : cg_residual_precs(g->prec, in->prec)) set_tuned_launch(g->prec, in->prec, in->LsE, cg_step_key(rp), L);
 }
 
@@ -85,9 +97,13 @@ using namespace gbdw;
 extern "C" {
 
 int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag) {
-  if (int st = check_operands(g, out, in, false)) return st;
+  // even-odd operands (gauge and out on one half lattice, in on the other) tune the even-odd
+  // hopping term and its Schur-complement epilogue under their own keys
+  const bool eo = g && in && g->lat && g->lat->parity >= 0 && in->lat == g->lat->partner;
+  if (int st = eo ? check_eo(g, out, in) : check_operands(g, out, in, false)) return st;
   if (!g->lat->fast) return GBDW_OK;  // the general-table kernel has a single shape
   if (int st = ensure_device()) return st;
+  const int ko = eo ? EO_KEY : 0;
   // candidate shapes: direct loads with 1/2/4 slices per thread, and the TMA-staged form
   // with the slice splits compiled for this precision and 2 or 4 stages
   std::vector<DhopLaunch> cands;
@@ -136,19 +152,32 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
   cudaEvent_t a, b;
   GBDW_CUDA(cudaEventCreate(&a));
   GBDW_CUDA(cudaEventCreate(&b));
-  const DhopLaunch saved = tuned_launch(g->prec, in->prec, in->LsE, 0);
+  gbdw_field* cen = nullptr;  // the even-odd M epilogue's diagonal field (on out's half)
+  if (eo && in->nrhs == 1) {
+    if (int st = gbdw_field_create(&cen, out->lat, in->prec, 1)) {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+      return st;
+    }
+  }
+  DhopLaunch saved = tuned_launch(g->prec, in->prec, in->LsE, 0);
+  if (eo) find_tuned_launch(g->prec, in->prec, in->LsE, ko, &saved);
   DhopLaunch best = saved, best_m = saved;
   float best_ms = 1e30f, best_m_ms = 1e30f;
   int status = GBDW_OK;
   // time reps launches of the hopping term (epi 0) or of M (epi 1) with shape L
+  auto apply = [&](int epi) -> int {
+    if (!eo) return run_dhop(g, out, in, dag, epi, 1.2, 0.01, nullptr);
+    return hop_eo(g, out, in, dag, epi ? cen : nullptr, 1.8, 0.01, epi ? 0.25 : 0.5, nullptr, true);
+  };
   auto time_shape = [&](const DhopLaunch& L, int epi, float* ms) -> int {
-    set_tuned_launch(g->prec, in->prec, in->LsE, epi, L);
+    set_tuned_launch(g->prec, in->prec, in->LsE, epi + ko, L);
     int st = GBDW_OK;
-    for (int w = 0; w < 3 && !st; ++w) st = run_dhop(g, out, in, dag, epi, 1.2, 0.01, nullptr);
+    for (int w = 0; w < 3 && !st; ++w) st = apply(epi);
     if (st) return st;
     const int reps = 10;
     cudaEventRecord(a, stream());
-    for (int r = 0; r < reps && !st; ++r) st = run_dhop(g, out, in, dag, epi, 1.2, 0.01, nullptr);
+    for (int r = 0; r < reps && !st; ++r) st = apply(epi);
     cudaEventRecord(b, stream());
     cudaEventSynchronize(b);
     if (st) return st;
@@ -159,7 +188,8 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
   // centre site's 5th-dimension neighbours, and the CG passes run on its shape with their
   // residual epilogues.  Measured at 32^4 x 16: the hopping term's best sweep (form 3 in t-bricks
   // of 8) cost the FP32 CG 7 % against the staged form that M alone prefers.
-  const DhopLaunch saved_m = tuned_launch(g->prec, in->prec, in->LsE, 1);
+  DhopLaunch saved_m = tuned_launch(g->prec, in->prec, in->LsE, 1);
+  if (eo) find_tuned_launch(g->prec, in->prec, in->LsE, 1 + ko, &saved_m);
   std::vector<std::pair<float, DhopLaunch>> m_times;
   for (const DhopLaunch& L : cands) {
     float ms = 0.f;
@@ -176,14 +206,15 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
       best_m = L;
     }
   }
-  set_tuned_launch(g->prec, in->prec, in->LsE, 0, status ? saved : best);
-  if (in->nrhs == 1) set_tuned_launch(g->prec, in->prec, in->LsE, 1, status ? saved_m : best_m);
+  set_tuned_launch(g->prec, in->prec, in->LsE, ko, status ? saved : best);
+  if (in->nrhs == 1) set_tuned_launch(g->prec, in->prec, in->LsE, 1 + ko, status ? saved_m : best_m);
+  if (cen) gbdw_field_destroy(cen);
   // The fused CG step (mdagm_residual: M with |Mp|^2 and alpha reduced, then M^dag with r updated
   // and |r|^2 reduced) reads and writes r besides M's traffic, so its best shape can differ from
   // M's (measured at 32^4 x 16 with an FP64 r: M alone fastest in t-bricks of 8 on form 3, the CG
   // step 7 % faster on the staged form).  It is timed on the real pass over a shortlist: M's four
   // fastest shapes and the fastest natural-order shape of each form.
-  if (!status && in->nrhs == 1 && !m_times.empty()) {
+  if (!status && !eo && in->nrhs == 1 && !m_times.empty()) {
     std::stable_sort(m_times.begin(), m_times.end(),
                      [](const std::pair<float, DhopLaunch>& x, const std::pair<float, DhopLaunch>& y) {
                        return x.first < y.first;
@@ -237,7 +268,7 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
 
 int gbdw_tune_query(const gbdw_gauge* g, const gbdw_field* in, int cfg[4]) {
   if (!g || !in || !cfg) return GBDW_ERR_INVALID;
-  const DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, 0);
+  const DhopLaunch L = lookup(g, in, 0);
   cfg[0] = L.threads;
   cfg[1] = L.spt;
   cfg[2] = L.mode;
@@ -247,7 +278,7 @@ int gbdw_tune_query(const gbdw_gauge* g, const gbdw_field* in, int cfg[4]) {
 
 int gbdw_tune_query_m(const gbdw_gauge* g, const gbdw_field* in, int cfg[6]) {
   if (!g || !in || !cfg) return GBDW_ERR_INVALID;
-  const DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, 1);
+  const DhopLaunch L = lookup(g, in, 1);
   const int v[6] = {L.threads, L.spt, L.mode, L.stages, L.split, L.brick};
   for (int i = 0; i < 6; ++i) cfg[i] = v[i];
   return GBDW_OK;
@@ -255,8 +286,8 @@ int gbdw_tune_query_m(const gbdw_gauge* g, const gbdw_field* in, int cfg[6]) {
 
 int gbdw_tune_query_cg(const gbdw_gauge* g, const gbdw_field* in, int rprec, int cfg[6]) {
   if (!g || !in || !cfg || rprec < GBDW_F64 || rprec > GBDW_F16) return GBDW_ERR_INVALID;
-  DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, 1);
-  find_tuned_launch(g->prec, in->prec, in->LsE, cg_step_key(rprec), &L);
+  DhopLaunch L = lookup(g, in, 1);
+  if (g->lat->parity < 0) find_tuned_launch(g->prec, in->prec, in->LsE, cg_step_key(rprec), &L);
   const int v[6] = {L.threads, L.spt, L.mode, L.stages, L.split, L.brick};
   for (int i = 0; i < 6; ++i) cfg[i] = v[i];
   return GBDW_OK;
@@ -296,13 +327,13 @@ int gbdw_tune_set(const gbdw_gauge* g, const gbdw_field* in, int threads, int sp
 
 int gbdw_tune_split(const gbdw_gauge* g, const gbdw_field* in, int* split) {
   if (!g || !in || !split) return GBDW_ERR_INVALID;
-  *split = tuned_launch(g->prec, in->prec, in->LsE, 0).split;
+  *split = lookup(g, in, 0).split;
   return GBDW_OK;
 }
 
 int gbdw_tune_set_split(const gbdw_gauge* g, const gbdw_field* in, int split) {
   if (!g || !in) return GBDW_ERR_INVALID;
-  DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, 0);
+  DhopLaunch L = lookup(g, in, 0);
   L.split = split;
   if (split < 1 || (split > 1 && tile_extent(in->LsE, L, false) == 0)) {
     set_error("gbdw_tune_set_split: the chosen form must be direct (0 or 3) and Ls*nrhs must split into whole "
@@ -315,13 +346,13 @@ int gbdw_tune_set_split(const gbdw_gauge* g, const gbdw_field* in, int split) {
 
 int gbdw_tune_brick(const gbdw_gauge* g, const gbdw_field* in, int* brick) {
   if (!g || !in || !brick) return GBDW_ERR_INVALID;
-  *brick = tuned_launch(g->prec, in->prec, in->LsE, 0).brick;
+  *brick = lookup(g, in, 0).brick;
   return GBDW_OK;
 }
 
 int gbdw_tune_set_brick(const gbdw_gauge* g, const gbdw_field* in, int brick) {
   if (!g || !in) return GBDW_ERR_INVALID;
-  DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, 0);
+  DhopLaunch L = lookup(g, in, 0);
   L.brick = brick;
   if (brick < 1 || (brick > 1 && brick_extent(g->lat, L) == 0)) {
     set_error("gbdw_tune_set_brick: the chosen form must be direct (0 or 3) on a periodic lattice whose Lt the "

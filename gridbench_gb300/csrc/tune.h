@@ -22,6 +22,9 @@ struct DhopExtra {
   // a tune-cache key to take the launch shape from when it holds one (else the epilogue's own)
   int tune_key = -1;
 };
+// tune-cache epilogue keys of the even-odd hopping term (half lattices) are offset by this; a half
+// lattice without its own entry takes the full lattice's
+constexpr int EO_KEY = 32;
 // tune-cache key of the fused CG step (both passes of mdagm_residual) with a residual of precision rprec
 inline int cg_step_key(int rprec) { return 16 + rprec; }
 // the cached shape for the key, if one was tuned or pinned

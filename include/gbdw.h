@@ -345,7 +345,10 @@ int gbdw_batch_set_shape(gbdw_batch* b, const int shape[4]);
 /* ------------------------------------------------------------------ autotuner
  * Times the launch shapes of the hopping kernel for (g, field) and stores the fastest in
  * the process cache and, if path is non-NULL, in a JSON file read back by gbdw_tune_load.
- * Untuned shapes use built-in defaults. */
+ * Untuned shapes use built-in defaults.  Even-odd operands (g and out on one half lattice, in on
+ * its partner, as gbdw_dhop_eo takes them) tune the even-odd hopping term and its Schur epilogue
+ * under keys of their own; a half lattice without them runs the full lattice's shapes.  The
+ * gbdw_tune_query / _set / _split / _brick calls on a half-lattice gauge field read and pin those. */
 int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag);
 int gbdw_tune_load(const char* path);
 int gbdw_tune_save(const char* path);
