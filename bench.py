@@ -313,6 +313,18 @@ def secondary(gb, args, peak) -> dict:
             if fp64_peak:
                 rec["fp64_peak_tflops"] = fp64_peak
                 rec["fp64_frac"] = round(rec["fp64_tflops"] / fp64_peak["value"], 3)
+            # the same FP64 fields through the double-single form (FP32-pair arithmetic)
+            gb.set_fp64_arith(gb.FP64_OPERATORS, gb.FP64_DOUBLE_SINGLE)
+            try:
+                ms, _ = time_dhop(gb, g, [(y, x)], steps, 5, dag)
+                t_ds = ms / steps / 1e3
+                rec["double_single"] = {
+                    "ms": round(t_ds * 1e3, 4), "gflops": round(FLOP_PER_SITE * V5 / t_ds / 1e9, 1),
+                    "hbm_frac": round(algo_bytes(0, 0, LS) * V5 / t_ds / 1e9 / peak, 3),
+                    "speedup_vs_fp64": round(t / t_ds, 2), "rel_err_vs_fp64": rel_to(gb, lat, y, ref),
+                    "launch": [128, 2, 0]}
+            finally:
+                gb.set_fp64_arith(gb.FP64_OPERATORS, gb.FP64_NATIVE)
         out[name] = rec
     # even-odd: the hopping term between half lattices and the closed-form D5^-1 (FP32)
     le, lo = lat.checkerboard()

@@ -13,8 +13,8 @@ from typing import Sequence
 import numpy as np
 
 from . import _native
-from ._native import (BF16, CG_DOUBLE, CG_MIXED, CG_PLAIN, F16, F32, F64, CGParams, CGStats, GbdwError,
-                      check, load)
+from ._native import (BF16, CG_DOUBLE, CG_MIXED, CG_PLAIN, F16, F32, F64, FP64_DOUBLE_SINGLE, FP64_NATIVE,
+                      FP64_OPERATORS, FP64_SOLVERS, CGParams, CGStats, GbdwError, check, load)
 
 __all__ = ["F64", "F32", "F16", "BF16", "CG_PLAIN", "CG_MIXED", "CG_DOUBLE", "GbdwError", "load",
            "device_available", "launch_count", "synchronize", "seed_from_ints", "generate_gauge",
@@ -511,6 +511,18 @@ def tune_brick(g: Gauge, inp: Field) -> int:
 
 def tune_set_brick(g: Gauge, inp: Field, brick: int):
     check(load().gbdw_tune_set_brick(g.h, inp.h, int(brick)))
+
+
+def set_fp64_arith(where: int, mode: int) -> None:
+    """FP64 operators in native FP64 (FP64_NATIVE) or on FP32 pairs (FP64_DOUBLE_SINGLE, ~1e-14
+    relative), for explicit operator calls (FP64_OPERATORS) or the solvers (FP64_SOLVERS)."""
+    check(load().gbdw_set_fp64_arith(int(where), int(mode)))
+
+
+def get_fp64_arith(where: int) -> int:
+    v = C.c_int()
+    check(load().gbdw_get_fp64_arith(int(where), C.byref(v)))
+    return v.value
 
 
 def tune_query_m(g: Gauge, inp: Field) -> tuple:

@@ -14,6 +14,8 @@ from . import build as _build
 OK, ERR_INVALID, ERR_CUDA, ERR_ALLOC, ERR_TABLE, ERR_NOT_CONVERGED, ERR_DIVERGED, ERR_NO_DEVICE = range(8)
 F64, F32, F16, BF16 = 0, 1, 2, 3
 CG_PLAIN, CG_MIXED, CG_DOUBLE = 0, 1, 2
+FP64_OPERATORS, FP64_SOLVERS = 0, 1
+FP64_NATIVE, FP64_DOUBLE_SINGLE = 0, 1
 
 ERR_TIMEOUT = 8
 STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "ALLOC", 4: "TABLE", 5: "NOT_CONVERGED",
@@ -126,6 +128,8 @@ PROTOTYPES = {
     "gbdw_tune_brick": (_i, [_vp, _vp, C.POINTER(C.c_int)]),
     "gbdw_tune_set_brick": (_i, [_vp, _vp, _i]),
     "gbdw_tune_query_m": (_i, [_vp, _vp, C.POINTER(C.c_int)]),
+    "gbdw_set_fp64_arith": (_i, [_i, _i]),
+    "gbdw_get_fp64_arith": (_i, [_i, C.POINTER(C.c_int)]),
     "gbdw_tune_query_cg": (_i, [_vp, _vp, _i, C.POINTER(C.c_int)]),
     "gbdw_selftest_wait_timeout": (_i, [_u64]),
     "gbdw_timer_create": (_i, [_pp]),

@@ -22,7 +22,7 @@ DRIVERS = os.path.join(PKG, "drivers")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_UNITS = ["context.cu", "fields.cu", "dhop.cu", "dhop_f32.cu", "dhop_f64.cu", "dhop_f16.cu",
+CUDA_UNITS = ["context.cu", "fields.cu", "dhop.cu", "dhop_f32.cu", "dhop_f64.cu", "dhop_f16.cu", "dhop_ds.cu",
               "blas.cu", "cg.cu", "batch.cu", "tune.cu", "dslash_api.cu", "gen_device.cu", "selftest.cu", "noalloc.cu",
               "eo.cu", "mobius.cu", "halo.cu"]
 HOST_UNITS = ["gen.cc", "static_data.cc"]

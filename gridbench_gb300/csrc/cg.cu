@@ -254,6 +254,7 @@ extern "C" int gbdw_cg_solve(const gbdw_gauge* g64, const gbdw_gauge* g32, const
     return GBDW_ERR_INVALID;
   }
   TRY(ensure_device());
+  SolverScope fp64_scope;  // the solvers' FP64 arithmetic setting applies from here
   const gbdw_lattice* lat = g64->lat;
   Fields F;
   gbdw_field *tmp64 = nullptr, *tmps = nullptr;
@@ -293,6 +294,7 @@ extern "C" int gbdw_cg_solve_mobius(const gbdw_gauge* g64, const gbdw_gauge* g32
     return GBDW_ERR_INVALID;
   }
   TRY(ensure_device());
+  SolverScope fp64_scope;  // the solvers' FP64 arithmetic setting applies from here
   const gbdw_lattice* lat = g64->lat;
   Fields F;
   gbdw_field *t64 = nullptr, *u64 = nullptr, *ts = nullptr, *us = nullptr;
@@ -346,6 +348,7 @@ extern "C" int gbdw_cg_solve_mobius_eo(const gbdw_gauge* const g64[2], const gbd
     return GBDW_ERR_INVALID;
   }
   TRY(ensure_device());
+  SolverScope fp64_scope;  // the solvers' FP64 arithmetic setting applies from here
   Fields F;
   gbdw_field *be = nullptr, *bo = nullptr, *te = nullptr, *ue = nullptr, *xo = nullptr, *co = nullptr;
   gbdw_field *to = nullptr, *po = nullptr, *pa = nullptr;
@@ -449,6 +452,7 @@ extern "C" int gbdw_cg_solve_eo(const gbdw_gauge* const g64[2], const gbdw_gauge
     return GBDW_ERR_INVALID;
   }
   TRY(ensure_device());
+  SolverScope fp64_scope;  // the solvers' FP64 arithmetic setting applies from here
   Fields F;
   gbdw_field *be = nullptr, *bo = nullptr, *te = nullptr, *ue = nullptr, *xo = nullptr, *co = nullptr;
   gbdw_field *tp64 = nullptr, *tq64 = nullptr;

@@ -73,6 +73,9 @@ struct gbdw_gauge {
   int prec;
   void* d;           // device storage
   size_t bytes;
+  // F64 gauge: the links split into FP32 pairs (re h, re l, im h, im l per entry) for the
+  // double-single operator, built on first use and freed with the gauge
+  mutable void* d_ds = nullptr;
 };
 
 struct gbdw_field {

@@ -176,6 +176,29 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
     p.result = red.result;
   }
   int st;
+  if (in->prec == GBDW_F64 && g->prec == GBDW_F64 && epi <= 1 && !p.mob && fp64_double_single()) {
+    // double-single arithmetic on the FP64 fields: direct form, its own fixed shape
+    if (int s2 = ds_links(g, &p.U)) return s2;
+    p.TE = 0;
+    p.brick = 0;
+    const DhopLaunch D{128, in->LsE % 2 == 0 ? 2 : 1};
+    const int64_t nthreads_ds = p.nsite * (p.LsE / D.spt);
+    const int64_t blocks_ds = (nthreads_ds + D.threads - 1) / D.threads;
+    if (reduce && blocks_ds != blocks) {
+      if (int s3 = reduce_scratch(blocks_ds, 1, &red)) return s3;
+      p.partials = red.partials;
+      p.counter = red.counter;
+      p.result = red.result;
+    }
+    st = launch_dhop_ds(p, dag, epi, D);
+    if (st) return st;
+    if (reduce) {
+      double* to = (ex && ex->sum_to) ? ex->sum_to : red.result;
+      if (int s2 = sum_partials(red.partials, blocks_ds, to, ex ? ex->num : 0.0, ex ? ex->alpha_to : nullptr)) return s2;
+      if (norm2 && fetch) return ex && ex->sum_to ? fetch_doubles(to, 1, norm2) : reduce_fetch(red, 1, norm2);
+    }
+    return GBDW_OK;
+  }
   if (in->prec == GBDW_F64) st = launch_dhop_f64(p, dag, epi, L);
   else if (in->prec == GBDW_F32) st = launch_dhop_f32(p, dag, epi, L);
   else st = launch_dhop_f16(p, g->prec, dag, epi, L);

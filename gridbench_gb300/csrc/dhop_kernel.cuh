@@ -32,6 +32,10 @@ template <>
 struct Arith<GBDW_F64> {
   using T = double;
 };
+template <>
+struct Arith<GBDW_DS> {
+  using T = dsf;
+};
 
 template <int N>
 __device__ __forceinline__ void load_norms(const float* nrm, int64_t e, float (&v)[N]) {
@@ -117,6 +121,20 @@ struct LinkIO<GBDW_F64> {
     for (int k = 0; k < 9; ++k) {
       const double2 a = ldv<SMEM>(p + k);
       u[k / 3][k % 3] = {a.x, a.y};
+    }
+  }
+};
+// the F64 gauge field's split copy: one float4 (re h, re l, im h, im l) per entry
+template <>
+struct LinkIO<GBDW_DS> {
+  static constexpr unsigned bytes = 144;
+  template <bool SMEM = false>
+  static __device__ __forceinline__ void load(const void* U, size_t link, cpx<dsf> (&u)[3][3]) {
+    const float4* p = (const float4*)U + link * 9;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      const float4 a = ldv<SMEM>(p + k);
+      u[k / 3][k % 3] = {dsf(a.x, a.y), dsf(a.z, a.w)};
     }
   }
 };
@@ -393,7 +411,7 @@ __device__ __forceinline__ void hop_leg_scalar(const cpx<T> (&u)[3][3], const vo
 // Accumulator of one thread: slice pairs for FP32/FP16 with even N, single slices otherwise.
 template <int PIN, int N>
 struct Acc {
-  static constexpr bool paired = PIN != GBDW_F64 && N % 2 == 0;
+  static constexpr bool paired = (PIN == GBDW_F32 || PIN == GBDW_F16) && N % 2 == 0;
   using T = typename Arith<PIN>::T;
   using Pair = cp2[N / 2 > 0 ? N / 2 : 1][12];
   using Single = cpx<T>[N][12];
@@ -544,6 +562,15 @@ template <int N>
 __device__ __forceinline__ double sumsq(const cpx<float> (&)[N][12]) {
   return 0.0;
 }
+template <int N>
+__device__ __forceinline__ double sumsq(const cpx<dsf> (&v)[N][12]) {
+  dsf s(0.f, 0.f);
+#pragma unroll
+  for (int j = 0; j < N; ++j)
+#pragma unroll
+    for (int k = 0; k < 12; ++k) s = fma(v[j][k].i, v[j][k].i, fma(v[j][k].r, v[j][k].r, s));
+  return double(s);
+}
 
 // ------------------------------------------------------------------ Shamir 5D terms
 // out(s) = a5 psi(s) - k D(s) - [P- psi(s+1) + P+ psi(s-1)]       (dag = 0)
@@ -660,7 +687,7 @@ __device__ __forceinline__ void mobius_adj_hop(const DhopParams& p, int s0, cpx<
 template <int PIN, int POUT, int DAG, int N, int EPI, class T>
 __device__ __forceinline__ void finish_site(const DhopParams& p, int64_t site, int s0, int LsE, int LsP,
                                             cpx<T> (&v)[N][12], float& part, double& dpart) {
-  if constexpr (EPI == 1 && DAG == 1 && N == 2) {
+  if constexpr (EPI == 1 && DAG == 1 && N == 2 && PIN != GBDW_DS) {
     if (p.mob) mobius_adj_hop(p, s0, v);
   }
   if constexpr (EPI >= 1) dwf_epilogue<PIN, DAG, N>(p, site, s0, v);
@@ -701,7 +728,7 @@ __device__ __forceinline__ void finish_site(const DhopParams& p, int64_t site, i
     dpart = s;
   } else {
     part = store_spinor<POUT, N>(p.out, p.out_norm, site, s0, LsE, LsP, v);
-    if constexpr (POUT == GBDW_F64) dpart = sumsq<N>(v);
+    if constexpr (POUT == GBDW_F64 || POUT == GBDW_DS) dpart = sumsq<N>(v);
   }
 }
 
@@ -803,7 +830,7 @@ __global__ void __launch_bounds__(MINB > 0 ? MAXT : 256, MINB > 0 ? MINB : 1) k_
     finish_site<PIN, POUT, DAG, N, EPI>(p, site, s0, p.LsE, p.LsP, acc, part, dpart);
   }
   if (p.partials) {
-    double v[1] = {(POUT == GBDW_F64 || (EPI >= 2 && EPI <= 4)) ? dpart : double(part)};
+    double v[1] = {(POUT == GBDW_F64 || POUT == GBDW_DS || (EPI >= 2 && EPI <= 4)) ? dpart : double(part)};
     block_partial<1>(v, p.partials);
   }
 }
@@ -853,6 +880,17 @@ int launch_dhop_f64(const DhopParams& p, int dag, int epi, DhopLaunch L);
 int launch_dhop_f32(const DhopParams& p, int dag, int epi, DhopLaunch L);
 int launch_dhop_f16(const DhopParams& p, int gprec, int dag, int epi, DhopLaunch L);
 int launch_dhop_general(const DhopParams& p, int prec, int dag);
+// The double-single form of the FP64 operator (dhop_ds.cu): direct loads, 1 or 2 slices per
+// thread, Dhop and M; p.U must be the gauge field's split links (ds_links).
+int launch_dhop_ds(const DhopParams& p, int dag, int epi, DhopLaunch L);
+int ds_links(const gbdw_gauge* g, const void** out);
+// whether FP64 operators run in double-single arithmetic here: the setting for solvers inside a
+// SolverScope (the solvers open one), the setting for operator calls outside
+bool fp64_double_single();
+struct SolverScope {
+  SolverScope();
+  ~SolverScope();
+};
 // Sites per CTA, threads and dynamic shared memory of a staged form (L.mode 1 or 2), or false
 // if that form cannot run for this precision and extent.
 bool tma_shape(int prec, int LsE, DhopLaunch L, int* NS, int* threads, size_t* smem);

@@ -498,6 +498,7 @@ int gbdw_gauge_destroy(gbdw_gauge* g) {
   if (!g) return GBDW_OK;
   cudaStreamSynchronize(stream());
   cudaFree(g->d);
+  if (g->d_ds) cudaFree(g->d_ds);
   delete g;
   return GBDW_OK;
 }

@@ -12,8 +12,13 @@
 // per-slice FP32 norm held in norm[site*LsE + e].
 #pragma once
 #include "common.cuh"
+#include "dsfloat.cuh"
 
 namespace gbdw {
+
+// Internal precision tag of the double-single operator: FP64 storage (the F64 layout), arithmetic
+// on FP32 pairs (dsfloat.cuh), links from the gauge field's split copy.
+constexpr int GBDW_DS = 7;
 
 __host__ __device__ inline int padded_slices(int prec, int LsE) {
   return prec == GBDW_F64 ? LsE : LsE + (LsE & 1);
@@ -69,6 +74,18 @@ struct Elem<GBDW_F32> {
     f[2] = im;
   }
 };
+// DS: FP64 storage, split into pairs on load and joined on store.
+template <>
+struct Elem<GBDW_DS> {
+  template <bool SMEM = false>
+  __device__ static cpx<dsf> ld(const void* b, int64_t row, int e, int LsP) {
+    const double2 a = ldv<SMEM>((const double2*)b + row * LsP + e);
+    return {ds_split(a.x), ds_split(a.y)};
+  }
+  __device__ static void st(void* b, int64_t row, int e, int LsP, dsf re, dsf im) {
+    ((double2*)b)[row * LsP + e] = make_double2(double(re), double(im));
+  }
+};
 // F16: returns / takes the stored (norm-scaled) values.
 template <>
 struct Elem<GBDW_F16> {
@@ -89,10 +106,10 @@ struct Elem<GBDW_F16> {
 // e0 % N == 0; for N >= 2 the slices come in whole pairs (e0 even).
 template <int P, int N, bool SMEM = false>
 struct Vec {
-  using T = typename std::conditional<P == GBDW_F64, double, float>::type;
+  using T = typename std::conditional<P == GBDW_F64, double, typename std::conditional<P == GBDW_DS, dsf, float>::type>::type;
 
   __device__ static void load(const void* b, int64_t row, int e0, int LsP, cpx<T> (&v)[N]) {
-    if constexpr (P == GBDW_F64 || N == 1) {
+    if constexpr (P == GBDW_F64 || P == GBDW_DS || N == 1) {
 #pragma unroll
       for (int j = 0; j < N; ++j) v[j] = Elem<P>::template ld<SMEM>(b, row, e0 + j, LsP);
     } else {
@@ -131,7 +148,7 @@ struct Vec {
   }
   // F64 / F32 stores
   __device__ static void store(void* b, int64_t row, int e0, int LsP, const cpx<T> (&v)[N]) {
-    if constexpr (P == GBDW_F64 || N == 1) {
+    if constexpr (P == GBDW_F64 || P == GBDW_DS || N == 1) {
 #pragma unroll
       for (int j = 0; j < N; ++j) Elem<P>::st(b, row, e0 + j, LsP, v[j].r, v[j].i);
     } else {

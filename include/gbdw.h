@@ -387,6 +387,18 @@ int gbdw_tune_query_m(const gbdw_gauge* g, const gbdw_field* in, int cfg[6]);
  * layout.  gbdw_tune_dhop times that step on a shortlist of M's fastest shapes; untuned, it is M's. */
 int gbdw_tune_query_cg(const gbdw_gauge* g, const gbdw_field* in, int rprec, int cfg[6]);
 
+/* ------------------------------------------------------------------ FP64 arithmetic
+ * GB300 executes FP64 at 1/64 of its FP32 rate, which leaves the FP64 hopping operator bound by
+ * its arithmetic, far from its memory roofline.  Its double-single form keeps the FP64 fields
+ * and gauge in memory and computes on FP32 pairs (~48 significant bits, ~1e-14 relative against
+ * FP64).  `where` selects the explicit FP64 operator calls (gbdw_dhop, gbdw_dwf_m, ... on F64
+ * fields; default GBDW_FP64_NATIVE) or the solvers' FP64 operator (true residuals, the FP64 CG;
+ * default GBDW_FP64_DOUBLE_SINGLE).  The setting is process-wide. */
+enum { GBDW_FP64_OPERATORS = 0, GBDW_FP64_SOLVERS = 1 };
+enum { GBDW_FP64_NATIVE = 0, GBDW_FP64_DOUBLE_SINGLE = 1 };
+int gbdw_set_fp64_arith(int where, int mode);
+int gbdw_get_fp64_arith(int where, int* mode);
+
 /* ------------------------------------------------------------------ timing on the library stream */
 typedef struct gbdw_timer gbdw_timer;
 int gbdw_timer_create(gbdw_timer** t);
