@@ -322,7 +322,7 @@ def secondary(gb, args, peak) -> dict:
                     "ms": round(t_ds * 1e3, 4), "gflops": round(FLOP_PER_SITE * V5 / t_ds / 1e9, 1),
                     "hbm_frac": round(algo_bytes(0, 0, LS) * V5 / t_ds / 1e9 / peak, 3),
                     "speedup_vs_fp64": round(t / t_ds, 2), "rel_err_vs_fp64": rel_to(gb, lat, y, ref),
-                    "launch": [128, 2, 0]}
+                    "launch": [128, 1, 0]}
             finally:
                 gb.set_fp64_arith(gb.FP64_OPERATORS, gb.FP64_NATIVE)
         out[name] = rec

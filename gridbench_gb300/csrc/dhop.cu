@@ -181,16 +181,14 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
     if (int s2 = ds_links(g, &p.U)) return s2;
     p.TE = 0;
     p.brick = 0;
-    const DhopLaunch D{128, in->LsE % 2 == 0 ? 2 : 1};
-    const int64_t nthreads_ds = p.nsite * (p.LsE / D.spt);
-    const int64_t blocks_ds = (nthreads_ds + D.threads - 1) / D.threads;
+    const int64_t blocks_ds = (p.nsite * p.LsE + DS_THREADS - 1) / DS_THREADS;
     if (reduce && blocks_ds != blocks) {
       if (int s3 = reduce_scratch(blocks_ds, 1, &red)) return s3;
       p.partials = red.partials;
       p.counter = red.counter;
       p.result = red.result;
     }
-    st = launch_dhop_ds(p, dag, epi, D);
+    st = launch_dhop_ds(p, dag, epi);
     if (st) return st;
     if (reduce) {
       double* to = (ex && ex->sum_to) ? ex->sum_to : red.result;

@@ -50,23 +50,20 @@ int ds_links(const gbdw_gauge* g, const void** out) {
   return GBDW_OK;
 }
 
-// Direct form, N = 1 or 2 slices per thread; Dhop and the M epilogue (with its fused norm).
-int launch_dhop_ds(const DhopParams& p, int dag, int epi, DhopLaunch L) {
+// Direct form, one slice per thread, 128-thread CTAs with registers capped for four CTAs per SM
+// (16 warps): the arithmetic is the bound, and warps hide its dependency chains.  Measured at
+// 16^4 x Ls=16 (Dhop, ms): 1.075 at this cap, 1.24 at three CTAs (170 registers), 1.79 uncapped
+// (254 registers, 8 warps); two slices per thread 1.80-2.56; native FP64 1.635.
+int launch_dhop_ds(const DhopParams& p, int dag, int epi) {
   if (epi > 1) {
     set_error("double-single operator: Dhop and M only");
     return GBDW_ERR_INVALID;
   }
-  const int N = (L.spt == 2 && p.LsE % 2 == 0) ? 2 : 1;
-  const int64_t nthreads = p.nsite * (p.LsE / N);
-  const unsigned blocks = unsigned((nthreads + L.threads - 1) / L.threads);
-#define GBDW_DSK(D, NN, E) k_dhop<GBDW_DS, GBDW_DS, GBDW_DS, D, NN, E><<<blocks, L.threads, 0, stream()>>>(p)
-  if (N == 2) {
-    if (dag) epi ? GBDW_DSK(1, 2, 1) : GBDW_DSK(1, 2, 0);
-    else epi ? GBDW_DSK(0, 2, 1) : GBDW_DSK(0, 2, 0);
-  } else {
-    if (dag) epi ? GBDW_DSK(1, 1, 1) : GBDW_DSK(1, 1, 0);
-    else epi ? GBDW_DSK(0, 1, 1) : GBDW_DSK(0, 1, 0);
-  }
+  const int64_t nthreads = p.nsite * p.LsE;
+  const unsigned blocks = unsigned((nthreads + DS_THREADS - 1) / DS_THREADS);
+#define GBDW_DSK(D, E) k_dhop<GBDW_DS, GBDW_DS, GBDW_DS, D, 1, E, 4, 0, DS_THREADS><<<blocks, DS_THREADS, 0, stream()>>>(p)
+  if (dag) epi ? GBDW_DSK(1, 1) : GBDW_DSK(1, 0);
+  else epi ? GBDW_DSK(0, 1) : GBDW_DSK(0, 0);
 #undef GBDW_DSK
   GBDW_LAUNCHED();
   return GBDW_OK;

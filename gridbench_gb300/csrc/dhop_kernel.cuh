@@ -880,9 +880,10 @@ int launch_dhop_f64(const DhopParams& p, int dag, int epi, DhopLaunch L);
 int launch_dhop_f32(const DhopParams& p, int dag, int epi, DhopLaunch L);
 int launch_dhop_f16(const DhopParams& p, int gprec, int dag, int epi, DhopLaunch L);
 int launch_dhop_general(const DhopParams& p, int prec, int dag);
-// The double-single form of the FP64 operator (dhop_ds.cu): direct loads, 1 or 2 slices per
-// thread, Dhop and M; p.U must be the gauge field's split links (ds_links).
-int launch_dhop_ds(const DhopParams& p, int dag, int epi, DhopLaunch L);
+// The double-single form of the FP64 operator (dhop_ds.cu): direct loads, one slice per thread in
+// CTAs of DS_THREADS, Dhop and M; p.U must be the gauge field's split links (ds_links).
+constexpr int DS_THREADS = 128;
+int launch_dhop_ds(const DhopParams& p, int dag, int epi);
 int ds_links(const gbdw_gauge* g, const void** out);
 // whether FP64 operators run in double-single arithmetic here: the setting for solvers inside a
 // SolverScope (the solvers open one), the setting for operator calls outside
