@@ -577,6 +577,17 @@ def bench_cg(gb, args) -> dict:
     g32 = gb.Gauge(lat, None, gb.F32, seed=77)
     g16 = gb.Gauge(lat, None, gb.F16, seed=77)
     m_shapes = {}
+    # the solvers' FP64 operator (true residuals) runs double-single: tune that form's shapes
+    gb.set_fp64_arith(gb.FP64_OPERATORS, gb.FP64_DOUBLE_SINGLE)
+    try:
+        x, y = gb.Field(lat, gb.F64).gaussian(1), gb.Field(lat, gb.F64)
+        gb.tune_dhop(g64, y, x)
+        m_shapes["fp64_double_single"] = {"dhop": list(gb.tune_query_ds(g64, x, 0)),
+                                          "m": list(gb.tune_query_ds(g64, x, 1)),
+                                          "fields": "CTAs per SM of the register cap, t-brick"}
+        del x, y
+    finally:
+        gb.set_fp64_arith(gb.FP64_OPERATORS, gb.FP64_NATIVE)
     for g, sp, tag in ((g32, gb.F32, "fp32"), (g16, gb.F16, "fp16")):
         x, y = gb.Field(lat, sp).gaussian(1), gb.Field(lat, sp)
         gb.tune_dhop(g, y, x)

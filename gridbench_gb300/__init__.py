@@ -519,6 +519,18 @@ def set_fp64_arith(where: int, mode: int) -> None:
     check(load().gbdw_set_fp64_arith(int(where), int(mode)))
 
 
+def tune_query_ds(g: Gauge, inp: Field, epi: int = 0) -> tuple:
+    """(CTAs per SM of the register cap, t-brick) of the double-single FP64 operator, for Dhop
+    (epi 0) or M (epi 1)."""
+    cfg = (C.c_int * 2)()
+    check(load().gbdw_tune_query_ds(g.h, inp.h, int(epi), cfg))
+    return tuple(int(v) for v in cfg)
+
+
+def tune_set_ds(g: Gauge, inp: Field, epi: int, minb: int, brick: int = 1) -> None:
+    check(load().gbdw_tune_set_ds(g.h, inp.h, int(epi), int(minb), int(brick)))
+
+
 def get_fp64_arith(where: int) -> int:
     v = C.c_int()
     check(load().gbdw_get_fp64_arith(int(where), C.byref(v)))

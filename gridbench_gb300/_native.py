@@ -130,6 +130,8 @@ PROTOTYPES = {
     "gbdw_tune_query_m": (_i, [_vp, _vp, C.POINTER(C.c_int)]),
     "gbdw_set_fp64_arith": (_i, [_i, _i]),
     "gbdw_get_fp64_arith": (_i, [_i, C.POINTER(C.c_int)]),
+    "gbdw_tune_query_ds": (_i, [_vp, _vp, _i, C.POINTER(C.c_int)]),
+    "gbdw_tune_set_ds": (_i, [_vp, _vp, _i, _i, _i]),
     "gbdw_tune_query_cg": (_i, [_vp, _vp, _i, C.POINTER(C.c_int)]),
     "gbdw_selftest_wait_timeout": (_i, [_u64]),
     "gbdw_timer_create": (_i, [_pp]),

@@ -179,8 +179,10 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
   if (in->prec == GBDW_F64 && g->prec == GBDW_F64 && epi <= 1 && !p.mob && fp64_double_single()) {
     // double-single arithmetic on the FP64 fields: direct form, its own fixed shape
     if (int s2 = ds_links(g, &p.U)) return s2;
+    DhopLaunch D{DS_THREADS, 1, 0, 4};  // stages: register cap as CTAs per SM
+    find_tuned_launch(g->prec, in->prec, in->LsE, tune_epi + DS_KEY, &D);
     p.TE = 0;
-    p.brick = 0;
+    p.brick = brick_extent(g->lat, DhopLaunch{DS_THREADS, 1, 0, 4, 1, D.brick});
     const int64_t blocks_ds = (p.nsite * p.LsE + DS_THREADS - 1) / DS_THREADS;
     if (reduce && blocks_ds != blocks) {
       if (int s3 = reduce_scratch(blocks_ds, 1, &red)) return s3;
@@ -188,7 +190,7 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
       p.counter = red.counter;
       p.result = red.result;
     }
-    st = launch_dhop_ds(p, dag, epi);
+    st = launch_dhop_ds(p, dag, epi, D.stages == 3 ? 3 : 4);
     if (st) return st;
     if (reduce) {
       double* to = (ex && ex->sum_to) ? ex->sum_to : red.result;

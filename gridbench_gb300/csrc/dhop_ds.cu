@@ -11,6 +11,7 @@ namespace gbdw {
 namespace {
 int g_mode[2] = {GBDW_FP64_NATIVE, GBDW_FP64_DOUBLE_SINGLE};  // operators, solvers
 thread_local int g_solver_depth = 0;
+thread_local int g_forced = -1;  // Fp64ArithOverride
 
 // one thread per link entry: FP64 complex -> (re h, re l, im h, im l)
 __global__ void k_split_links(const double2* __restrict__ U, float4* __restrict__ out, int64_t n) {
@@ -25,7 +26,13 @@ __global__ void k_split_links(const double2* __restrict__ U, float4* __restrict_
 SolverScope::SolverScope() { ++g_solver_depth; }
 SolverScope::~SolverScope() { --g_solver_depth; }
 
-bool fp64_double_single() { return g_mode[g_solver_depth > 0 ? 1 : 0] == GBDW_FP64_DOUBLE_SINGLE; }
+Fp64ArithOverride::Fp64ArithOverride(int mode) : prev(g_forced) { g_forced = mode; }
+Fp64ArithOverride::~Fp64ArithOverride() { g_forced = prev; }
+
+bool fp64_double_single() {
+  if (g_forced >= 0) return g_forced == GBDW_FP64_DOUBLE_SINGLE;
+  return g_mode[g_solver_depth > 0 ? 1 : 0] == GBDW_FP64_DOUBLE_SINGLE;
+}
 
 int ds_links(const gbdw_gauge* g, const void** out) {
   if (g->prec != GBDW_F64) {
@@ -54,16 +61,23 @@ int ds_links(const gbdw_gauge* g, const void** out) {
 // (16 warps): the arithmetic is the bound, and warps hide its dependency chains.  Measured at
 // 16^4 x Ls=16 (Dhop, ms): 1.075 at this cap, 1.24 at three CTAs (170 registers), 1.79 uncapped
 // (254 registers, 8 warps); two slices per thread 1.80-2.56; native FP64 1.635.
-int launch_dhop_ds(const DhopParams& p, int dag, int epi) {
-  if (epi > 1) {
-    set_error("double-single operator: Dhop and M only");
+// minb: the register cap, as CTAs per SM (4: 128 registers; 3: 170, which spills less in the M
+// epilogue); the t-brick order comes in p.brick.
+int launch_dhop_ds(const DhopParams& p, int dag, int epi, int minb) {
+  if (epi > 1 || (minb != 3 && minb != 4)) {
+    set_error("double-single operator: Dhop and M, three or four CTAs per SM");
     return GBDW_ERR_INVALID;
   }
   const int64_t nthreads = p.nsite * p.LsE;
   const unsigned blocks = unsigned((nthreads + DS_THREADS - 1) / DS_THREADS);
-#define GBDW_DSK(D, E) k_dhop<GBDW_DS, GBDW_DS, GBDW_DS, D, 1, E, 4, 0, DS_THREADS><<<blocks, DS_THREADS, 0, stream()>>>(p)
-  if (dag) epi ? GBDW_DSK(1, 1) : GBDW_DSK(1, 0);
-  else epi ? GBDW_DSK(0, 1) : GBDW_DSK(0, 0);
+#define GBDW_DSK(D, E, MB) k_dhop<GBDW_DS, GBDW_DS, GBDW_DS, D, 1, E, MB, 0, DS_THREADS><<<blocks, DS_THREADS, 0, stream()>>>(p)
+  if (minb == 4) {
+    if (dag) epi ? GBDW_DSK(1, 1, 4) : GBDW_DSK(1, 0, 4);
+    else epi ? GBDW_DSK(0, 1, 4) : GBDW_DSK(0, 0, 4);
+  } else {
+    if (dag) epi ? GBDW_DSK(1, 1, 3) : GBDW_DSK(1, 0, 3);
+    else epi ? GBDW_DSK(0, 1, 3) : GBDW_DSK(0, 0, 3);
+  }
 #undef GBDW_DSK
   GBDW_LAUNCHED();
   return GBDW_OK;

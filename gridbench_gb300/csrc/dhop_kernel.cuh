@@ -881,9 +881,12 @@ int launch_dhop_f32(const DhopParams& p, int dag, int epi, DhopLaunch L);
 int launch_dhop_f16(const DhopParams& p, int gprec, int dag, int epi, DhopLaunch L);
 int launch_dhop_general(const DhopParams& p, int prec, int dag);
 // The double-single form of the FP64 operator (dhop_ds.cu): direct loads, one slice per thread in
-// CTAs of DS_THREADS, Dhop and M; p.U must be the gauge field's split links (ds_links).
+// CTAs of DS_THREADS with registers capped for minb (3 or 4) CTAs per SM, Dhop and M; p.U must be
+// the gauge field's split links (ds_links).  Its tuned shapes sit in the tune cache under the
+// epilogue keys offset by DS_KEY, with `stages` holding minb and `brick` the t-brick order.
 constexpr int DS_THREADS = 128;
-int launch_dhop_ds(const DhopParams& p, int dag, int epi);
+constexpr int DS_KEY = 64;
+int launch_dhop_ds(const DhopParams& p, int dag, int epi, int minb);
 int ds_links(const gbdw_gauge* g, const void** out);
 // whether FP64 operators run in double-single arithmetic here: the setting for solvers inside a
 // SolverScope (the solvers open one), the setting for operator calls outside
@@ -891,6 +894,12 @@ bool fp64_double_single();
 struct SolverScope {
   SolverScope();
   ~SolverScope();
+};
+// forces one FP64 arithmetic (GBDW_FP64_NATIVE / _DOUBLE_SINGLE) on this thread while alive
+struct Fp64ArithOverride {
+  explicit Fp64ArithOverride(int mode);
+  ~Fp64ArithOverride();
+  int prev;
 };
 // Sites per CTA, threads and dynamic shared memory of a staged form (L.mode 1 or 2), or false
 // if that form cannot run for this precision and extent.

@@ -149,6 +149,10 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
       }
   }
   if (blocked_ok(g->lat, in)) cands.push_back(DhopLaunch{128, 2, 4, 4});
+  // FP64 fields whose operator calls run the double-single form (gbdw_set_fp64_arith): only that
+  // form's shapes are timed
+  const bool ds_only = in->prec == GBDW_F64 && g->prec == GBDW_F64 && !eo && fp64_double_single();
+  if (ds_only) cands.clear();
   cudaEvent_t a, b;
   GBDW_CUDA(cudaEventCreate(&a));
   GBDW_CUDA(cudaEventCreate(&b));
@@ -206,8 +210,39 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
       best_m = L;
     }
   }
-  set_tuned_launch(g->prec, in->prec, in->LsE, ko, status ? saved : best);
-  if (in->nrhs == 1) set_tuned_launch(g->prec, in->prec, in->LsE, 1 + ko, status ? saved_m : best_m);
+  if (!ds_only) {
+    set_tuned_launch(g->prec, in->prec, in->LsE, ko, status ? saved : best);
+    if (in->nrhs == 1) set_tuned_launch(g->prec, in->prec, in->LsE, 1 + ko, status ? saved_m : best_m);
+  }
+  // FP64 fields: the double-single form's register cap (three or four CTAs per SM) and t-brick
+  // order, for Dhop and M, timed with that form forced
+  if (!status && ds_only) {
+    Fp64ArithOverride force(GBDW_FP64_DOUBLE_SINGLE);
+    for (int epi = 0; epi <= (in->nrhs == 1 ? 1 : 0) && !status; ++epi) {
+      DhopLaunch best_ds{DS_THREADS, 1, 0, 4};
+      float best_ds_ms = 1e30f;
+      for (int minb : {4, 3})
+        for (int brick : {1, 2, 4, 8}) {
+          const DhopLaunch L{DS_THREADS, 1, 0, minb, 1, brick};
+          if (brick > 1 && brick_extent(g->lat, L) == 0) continue;
+          set_tuned_launch(g->prec, in->prec, in->LsE, epi + DS_KEY, L);
+          for (int w = 0; w < 2 && !status; ++w) status = apply(epi);
+          if (status) break;
+          cudaEventRecord(a, stream());
+          for (int r = 0; r < 5 && !status; ++r) status = apply(epi);
+          cudaEventRecord(b, stream());
+          cudaEventSynchronize(b);
+          if (status) break;
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, a, b);
+          if (ms < best_ds_ms) {
+            best_ds_ms = ms;
+            best_ds = L;
+          }
+        }
+      set_tuned_launch(g->prec, in->prec, in->LsE, epi + DS_KEY, best_ds);
+    }
+  }
   if (cen) gbdw_field_destroy(cen);
   // The fused CG step (mdagm_residual: M with |Mp|^2 and alpha reduced, then M^dag with r updated
   // and |r|^2 reduced) reads and writes r besides M's traffic, so its best shape can differ from
@@ -290,6 +325,26 @@ int gbdw_tune_query_cg(const gbdw_gauge* g, const gbdw_field* in, int rprec, int
   if (g->lat->parity < 0) find_tuned_launch(g->prec, in->prec, in->LsE, cg_step_key(rprec), &L);
   const int v[6] = {L.threads, L.spt, L.mode, L.stages, L.split, L.brick};
   for (int i = 0; i < 6; ++i) cfg[i] = v[i];
+  return GBDW_OK;
+}
+
+int gbdw_tune_query_ds(const gbdw_gauge* g, const gbdw_field* in, int epi, int cfg[2]) {
+  if (!g || !in || !cfg || epi < 0 || epi > 1) return GBDW_ERR_INVALID;
+  DhopLaunch L{DS_THREADS, 1, 0, 4};
+  find_tuned_launch(g->prec, in->prec, in->LsE, epi + DS_KEY, &L);
+  cfg[0] = L.stages;
+  cfg[1] = L.brick;
+  return GBDW_OK;
+}
+
+int gbdw_tune_set_ds(const gbdw_gauge* g, const gbdw_field* in, int epi, int minb, int brick) {
+  if (!g || !in || epi < 0 || epi > 1 || (minb != 3 && minb != 4) || brick < 1) return GBDW_ERR_INVALID;
+  const DhopLaunch L{DS_THREADS, 1, 0, minb, 1, brick};
+  if (brick > 1 && brick_extent(g->lat, L) == 0) {
+    set_error("gbdw_tune_set_ds: a t-brick needs a periodic lattice whose Lt it divides");
+    return GBDW_ERR_INVALID;
+  }
+  set_tuned_launch(g->prec, in->prec, in->LsE, epi + DS_KEY, L);
   return GBDW_OK;
 }
 

@@ -398,6 +398,11 @@ enum { GBDW_FP64_OPERATORS = 0, GBDW_FP64_SOLVERS = 1 };
 enum { GBDW_FP64_NATIVE = 0, GBDW_FP64_DOUBLE_SINGLE = 1 };
 int gbdw_set_fp64_arith(int where, int mode);
 int gbdw_get_fp64_arith(int where, int* mode);
+/* gbdw_tune_dhop on F64 fields while explicit operators run double-single tunes that form's
+ * shapes (used by the solvers as well): cfg[2] = CTAs per SM the registers are capped for (3 or
+ * 4) and the t-brick sweep order, for Dhop (epi 0) or M (epi 1). */
+int gbdw_tune_query_ds(const gbdw_gauge* g, const gbdw_field* in, int epi, int cfg[2]);
+int gbdw_tune_set_ds(const gbdw_gauge* g, const gbdw_field* in, int epi, int minb, int brick);
 
 /* ------------------------------------------------------------------ timing on the library stream */
 typedef struct gbdw_timer gbdw_timer;

@@ -53,6 +53,34 @@ def test_ds_dhop_matches_oracle(ds_ops, dims, Ls, dag):
         assert rel_err(out, nat) < TOL
 
 
+@pytest.mark.parametrize("minb,brick", [(4, 1), (3, 1), (4, 2), (3, 4), (4, 8)])
+def test_ds_register_caps_and_t_bricks(ds_ops, minb, brick):
+    """Each register cap and t-brick sweep order of the double-single kernel, Dhop and M, and
+    the tuner's own pick."""
+    dims, Ls = (4, 4, 4, 8), 8
+    c = make_case(dims, Ls)
+    lat = gb.Lattice.periodic(dims, Ls)
+    g = gb.Gauge(lat, c["U"], gb.F64)
+    x, y = gb.Field(lat, gb.F64).load(c["phi"]), gb.Field(lat, gb.F64)
+    gb.tune_set_ds(g, x, 0, minb, brick)
+    gb.tune_set_ds(g, x, 1, minb, brick)
+    assert gb.tune_query_ds(g, x, 0) == (minb, brick)
+    for dag in (0, 1):
+        gb.dhop(g, y, x, dag)
+        ref = oracle.dslash(c["U"], c["phi"], c["nbr"], c["prm"], c["nsite"], Ls, dag)
+        assert rel_err(y.numpy(), ref) < TOL, (minb, brick, dag)
+        gb.dwf_m(g, y, x, M5, MF, dag)
+        refm = oracle.dwf_m(c["U"], c["phi"], c["nbr"], c["nsite"], Ls, M5, MF, dag)
+        assert rel_err(y.numpy(), refm) < TOL, (minb, brick, dag)
+    gb.tune_dhop(g, y, x)
+    m, b = gb.tune_query_ds(g, x, 1)
+    assert m in (3, 4) and b in (1, 2, 4, 8)
+    gb.dwf_m(g, y, x, M5, MF, 0)
+    assert rel_err(y.numpy(), oracle.dwf_m(c["U"], c["phi"], c["nbr"], c["nsite"], Ls, M5, MF, 0)) < TOL
+    with pytest.raises(gb.GbdwError):
+        gb.tune_set_ds(g, x, 0, 4, 3)  # Lt = 8 is no multiple of 3
+
+
 def test_ds_multi_rhs(ds_ops):
     dims, Ls, k = (4, 4, 2, 4), 4, 3  # Ls * nrhs = 12 (pairs) and 3 right-hand sides
     c = make_case(dims, Ls)
