@@ -1,6 +1,6 @@
 """The double-single form of the FP64 operator (FP64 fields and gauge, arithmetic on FP32 pairs)
-against the FP64 oracle: Dhop and DhopDag on periodic and table lattices (one and two slices per
-thread, several right-hand sides), M with its fused norm, the even-odd hopping term and the
+against the FP64 oracle: Dhop and DhopDag on periodic and table lattices (each register cap and
+t-brick order, several right-hand sides), M with its fused norm, the even-odd hopping term and the
 Schur epilogue, at the FP64 tolerance (1e-12 relative) and the reference's own acceptance sum
 (sum of squared differences <= 1e-10, bench_simple.cc:114-119).  The setting is restored after
 each test; the solvers' default (double-single) is covered by the CG tests."""
