@@ -821,6 +821,9 @@ ONLY = {  # name -> (dims, Ls, spinor precision, gauge precision, dag[, right-ha
     "dhop_f16": (DIMS, LS, 2, 2, 0), "dhop_bf16": (DIMS, LS, 2, 3, 0),
     # the 12-RHS kernel on a lattice small enough for a full profile (2 x 0.9 GB fields)
     "dhop_f32_12rhs_16x12": (DIMS, 12, 1, 1, 0, 12),
+    # FP64 fields through the double-single form, at the shape its tuner picks at 16^4 x 16
+    # (registers capped for four CTAs per SM, natural order)
+    "dhop_f64ds": (DIMS, LS, 0, 0, 0),
 }
 
 
@@ -872,7 +875,10 @@ def run_only(args) -> dict:
         for r in range(k):
             x.gaussian(21 + i + 2 * r, r)
     ys = [gb.Field(lat, sp, k) for _ in range(2)]
-    if args.shape:
+    if args.only == "dhop_f64ds":
+        gb.set_fp64_arith(gb.FP64_OPERATORS, gb.FP64_DOUBLE_SINGLE)
+        gb.tune_set_ds(g, xs[0], 0, 4, 1)
+    elif args.shape:
         th, spt, form, st = (int(v) for v in args.shape.split(","))
         gb.tune_set(g, xs[0], th, spt, form, st)
     else:
