@@ -734,73 +734,9 @@ __device__ __forceinline__ void finish_site(const DhopParams& p, int64_t site, i
 
 // ------------------------------------------------------------------ kernels
 // Hopping sum for one thread: site and first slice s0 of N consecutive slices.
-// Double-single legs.  Eight unrolled double-single leg bodies overflow the instruction cache
-// (the kernel stalled on instruction fetch more than on anything else), so the legs run in two
-// runtime loops, X/Y legs and Z/T legs, whose projection rows (A, B) are compile-time; the unit
-// coefficients of each leg (the LegSpin table) are selected at run time.
-__device__ __forceinline__ dsf ds_neg_if(dsf a, bool n) { return n ? dsf(-a.h, -a.l) : a; }
-// c * a for c = +1, -1, +i, -i (codes 0..3)
-__device__ __forceinline__ cpx<dsf> ds_unit(int c, cpx<dsf> a) {
-  const bool sw = c >= 2;
-  const cpx<dsf> b = {sw ? a.i : a.r, sw ? a.r : a.i};
-  return {ds_neg_if(b.r, c == 1 || c == 2), ds_neg_if(b.i, c == 1 || c == 3)};
-}
-template <int DAG, int A, int B>
-__device__ __forceinline__ void ds_leg(const DhopParams& p, unsigned site, int L, int s0, cpx<dsf> (&acc)[12]) {
-  // the leg's unit codes, as LegSpin<DAG ? L ^ 4 : L> has them
-  const int LT = DAG ? (L ^ 4) : L;
-  const int d = LT & 3;
-  const int c0p = d == 0 ? 3 : d == 1 ? 0 : d == 2 ? 3 : 1;
-  const int c1p = d == 0 ? 3 : d == 1 ? 1 : d == 2 ? 2 : 1;
-  const int C0 = LT < 4 ? c0p : (c0p ^ 1), C1 = LT < 4 ? c1p : (c1p ^ 1);
-  const int K0 = C0 == 2 ? 3 : C0 == 3 ? 2 : C0, K1 = C1 == 2 ? 3 : C1 == 3 ? 2 : C1;  // conjugates
-  const int64_t n = __ldg(p.nbr4 + size_t(site) * 8 + L);
-  const int64_t row0 = n * 12;
-  cpx<dsf> u[3][3];
-  LinkIO<GBDW_DS>::load(p.U, size_t(site) * 8 + L, u);
-  cpx<dsf> h0[3], h1[3];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    const cpx<dsf> x = Elem<GBDW_DS>::ld(p.in, row0 + 0 * 3 + c, s0, p.LsP);
-    const cpx<dsf> y = ds_unit(C0, Elem<GBDW_DS>::ld(p.in, row0 + A * 3 + c, s0, p.LsP));
-    const cpx<dsf> z = Elem<GBDW_DS>::ld(p.in, row0 + 1 * 3 + c, s0, p.LsP);
-    const cpx<dsf> w = ds_unit(C1, Elem<GBDW_DS>::ld(p.in, row0 + B * 3 + c, s0, p.LsP));
-    h0[c] = {x.r + y.r, x.i + y.i};
-    h1[c] = {z.r + w.r, z.i + w.i};
-  }
-#pragma unroll
-  for (int r = 0; r < 3; ++r) {
-    cpx<dsf> u0 = {dsf(0.f, 0.f), dsf(0.f, 0.f)}, u1 = u0;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      cmac(u0, u[r][c], h0[c]);
-      cmac(u1, u[r][c], h1[c]);
-    }
-    const cpx<dsf> ra = ds_unit(K0, u0), rb = ds_unit(K1, u1);
-    acc[0 * 3 + r] = {acc[0 * 3 + r].r + u0.r, acc[0 * 3 + r].i + u0.i};
-    acc[1 * 3 + r] = {acc[1 * 3 + r].r + u1.r, acc[1 * 3 + r].i + u1.i};
-    acc[A * 3 + r] = {acc[A * 3 + r].r + ra.r, acc[A * 3 + r].i + ra.i};
-    acc[B * 3 + r] = {acc[B * 3 + r].r + rb.r, acc[B * 3 + r].i + rb.i};
-  }
-}
-template <int DAG>
-__device__ __forceinline__ void dhop_thread_ds(const DhopParams& p, unsigned site, int s0, cpx<dsf> (&out)[1][12]) {
-#pragma unroll
-  for (int k = 0; k < 12; ++k) out[0][k] = {dsf(0.f, 0.f), dsf(0.f, 0.f)};
-  // X+, X-, Y+, Y- (rows A = 3, B = 2), then Z+, Z-, T+, T- (A = 2, B = 3)
-#pragma unroll 1
-  for (int k = 0; k < 4; ++k) ds_leg<DAG, 3, 2>(p, site, (k >> 1) + ((k & 1) << 2), s0, out[0]);
-#pragma unroll 1
-  for (int k = 0; k < 4; ++k) ds_leg<DAG, 2, 3>(p, site, 2 + (k >> 1) + ((k & 1) << 2), s0, out[0]);
-}
-
 template <int PIN, int GP, int DAG, int N, bool MOB = false>
 __device__ __forceinline__ void dhop_thread(const DhopParams& p, unsigned site, int s0,
                                             cpx<typename Arith<PIN>::T> (&out)[N][12]) {
-  if constexpr (PIN == GBDW_DS && N == 1) {
-    dhop_thread_ds<DAG>(p, site, s0, out);
-    return;
-  }
   using T = typename Arith<PIN>::T;
   Acc<PIN, N> acc;
   acc.zero();
