@@ -149,8 +149,11 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
     set_error("device error word allocation failed");
     return GBDW_ERR_ALLOC;
   }
-  DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, tune_epi);
-  if (g->lat->parity >= 0) find_tuned_launch(g->prec, in->prec, in->LsE, tune_epi + EO_KEY, &L);
+  // the forward Mobius M (A(b, c) on the loaded neighbours) has the hopping term's access pattern
+  // and no Shamir epilogue: it runs on the hopping term's shape
+  const int key_epi = (p.mob && epi == 6) ? 0 : tune_epi;
+  DhopLaunch L = tuned_launch(g->prec, in->prec, in->LsE, key_epi);
+  if (g->lat->parity >= 0) find_tuned_launch(g->prec, in->prec, in->LsE, key_epi + EO_KEY, &L);
   if (ex && ex->tune_key >= 0) find_tuned_launch(g->prec, in->prec, in->LsE, ex->tune_key, &L);
   if (in->LsE % L.spt != 0) L.spt = 1;
   if (p.mob) L.spt = 2;  // the fused adjoint works on slice pairs, one site's pairs in consecutive lanes
