@@ -126,3 +126,27 @@ def test_allocation_failure_injection_argument_checks():
     assert L.gbdw_debug_fail_allocs(-1, 1) == _native.ERR_INVALID
     assert L.gbdw_debug_fail_allocs(0, -2) == _native.ERR_INVALID
     assert L.gbdw_debug_fail_allocs(0, 0) == _native.OK
+
+
+def test_fp64_arithmetic_setting_without_a_device():
+    """The FP64 arithmetic setting is host state: defaults (explicit operators native, solvers
+    double-single), round trip, and rejection of unknown selectors and modes."""
+    assert gb.get_fp64_arith(gb.FP64_OPERATORS) == gb.FP64_NATIVE
+    assert gb.get_fp64_arith(gb.FP64_SOLVERS) == gb.FP64_DOUBLE_SINGLE
+    try:
+        gb.set_fp64_arith(gb.FP64_OPERATORS, gb.FP64_DOUBLE_SINGLE)
+        assert gb.get_fp64_arith(gb.FP64_OPERATORS) == gb.FP64_DOUBLE_SINGLE
+        gb.set_fp64_arith(gb.FP64_SOLVERS, gb.FP64_NATIVE)
+        assert gb.get_fp64_arith(gb.FP64_SOLVERS) == gb.FP64_NATIVE
+    finally:
+        gb.set_fp64_arith(gb.FP64_OPERATORS, gb.FP64_NATIVE)
+        gb.set_fp64_arith(gb.FP64_SOLVERS, gb.FP64_DOUBLE_SINGLE)
+    L = gb.load()
+    assert L.gbdw_set_fp64_arith(2, gb.FP64_NATIVE) == _native.ERR_INVALID
+    assert L.gbdw_set_fp64_arith(gb.FP64_OPERATORS, 2) == _native.ERR_INVALID
+    assert L.gbdw_get_fp64_arith(gb.FP64_OPERATORS, None) == _native.ERR_INVALID
+    # the tuner queries reject null operands before touching a device
+    assert L.gbdw_tune_query_ds(None, None, 0, None) == _native.ERR_INVALID
+    assert L.gbdw_tune_set_ds(None, None, 0, 4, 1) == _native.ERR_INVALID
+    assert L.gbdw_tune_query_m(None, None, None) == _native.ERR_INVALID
+    assert L.gbdw_tune_query_cg(None, None, gb.F64, None) == _native.ERR_INVALID
