@@ -189,9 +189,7 @@ int gbdw_tune_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, i
     return GBDW_OK;
   };
   // M (one right-hand side) is timed over the same shapes on its own: its epilogue reads the
-  // centre site's 5th-dimension neighbours, and the CG passes run on its shape with their
-  // residual epilogues.  Measured at 32^4 x 16: the hopping term's best sweep (form 3 in t-bricks
-  // of 8) cost the FP32 CG 7 % against the staged form that M alone prefers.
+  // centre site and its 5th-dimension neighbours besides the hopping term's gather.
   DhopLaunch saved_m = tuned_launch(g->prec, in->prec, in->LsE, 1);
   if (eo) find_tuned_launch(g->prec, in->prec, in->LsE, 1 + ko, &saved_m);
   std::vector<std::pair<float, DhopLaunch>> m_times;
