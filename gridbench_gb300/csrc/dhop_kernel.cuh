@@ -389,22 +389,10 @@ __device__ __forceinline__ void hop_leg_scalar(const cpx<T> (&u)[3][3], const vo
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
       cpx<T> u0 = {T(0), T(0)}, u1 = {T(0), T(0)};
-      if constexpr (std::is_same<T, dsf>::value) {
-        // double-single: each real of U h as one compensated 6-term dot product
-        const dsf ur[6] = {u[r][0].r, u[r][1].r, u[r][2].r, -u[r][0].i, -u[r][1].i, -u[r][2].i};
-        const dsf ui[6] = {u[r][0].r, u[r][1].r, u[r][2].r, u[r][0].i, u[r][1].i, u[r][2].i};
-        const dsf a0[6] = {h0[j][0].r, h0[j][1].r, h0[j][2].r, h0[j][0].i, h0[j][1].i, h0[j][2].i};
-        const dsf b0[6] = {h0[j][0].i, h0[j][1].i, h0[j][2].i, h0[j][0].r, h0[j][1].r, h0[j][2].r};
-        const dsf a1[6] = {h1[j][0].r, h1[j][1].r, h1[j][2].r, h1[j][0].i, h1[j][1].i, h1[j][2].i};
-        const dsf b1[6] = {h1[j][0].i, h1[j][1].i, h1[j][2].i, h1[j][0].r, h1[j][1].r, h1[j][2].r};
-        u0 = {ds_dot<6>(ur, a0), ds_dot<6>(ui, b0)};
-        u1 = {ds_dot<6>(ur, a1), ds_dot<6>(ui, b1)};
-      } else {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          cmac(u0, u[r][c], h0[j][c]);
-          cmac(u1, u[r][c], h1[j][c]);
-        }
+      for (int c = 0; c < 3; ++c) {
+        cmac(u0, u[r][c], h0[j][c]);
+        cmac(u1, u[r][c], h1[j][c]);
       }
       const cpx<T> ra = cunit<conj_unit<S::C0>::v>(u0);
       const cpx<T> rb = cunit<conj_unit<S::C1>::v>(u1);

@@ -142,51 +142,6 @@ GBDW_HD dsf ds_split(double d) {
 
 GBDW_HD dsf::dsf(double d) : dsf(ds_split(d)) {}
 
-// The split of the loads: the same value in fewer integer operations, for magnitudes in
-// [2^-126, 2^128) (others take ds_split).  h keeps the leading 24 bits (the FP64 exponent rebiased
-// in one 64-bit subtraction), l the remaining 29 bits rounded to 24 and scaled by the FP64 ulp
-// 2^(E-52), built from h's exponent field; the pair is left unnormalised (|l| < ulp(h)), which
-// the operations below accept.
-GBDW_HD dsf ds_split_load(double d) {
-  using namespace ds_detail;
-  const uint64_t b = bits(d);
-  const uint32_t e = uint32_t(b >> 52) & 0x7ffu;
-  if (e - 897u > 253u) return ds_split(d);
-  const uint32_t sgn = uint32_t(b >> 32) & 0x80000000u;
-  // bits 33..23 of b >> 29 hold the exponent, 22..0 the leading 23 mantissa bits
-  const uint32_t hb = uint32_t((b >> 29) - (uint64_t(896) << 23)) | sgn;
-  float l = 0.f;
-  if (e >= 949u) l = mul_(float(uint32_t(b) & 0x1fffffffu), from_bits(((hb & 0x7f800000u) - (52u << 23)) | sgn));
-  return {from_bits(hb), l};
-}
-
-// Exact product a.h * b.h = p + e, with the cross terms a.h b.l + a.l b.h added to e.
-GBDW_HD void ds_prod(dsf a, dsf b, float& p, float& e) {
-  using namespace ds_detail;
-  p = mul_(a.h, b.h);
-  e = fma_(a.h, b.h, -p);
-  e = fma_(a.h, b.l, e);
-  e = fma_(a.l, b.h, e);
-}
-// sum_i a[i] * b[i] over K terms: exact leading products summed by two_sum, every error term
-// collected in one FP32 word, one renormalisation at the end.  Error below 2^-45 of
-// sum_i |a[i] b[i]| for K <= 6.
-template <int K>
-GBDW_HD dsf ds_dot(const dsf (&a)[K], const dsf (&b)[K]) {
-  using namespace ds_detail;
-  float s, E;
-  ds_prod(a[0], b[0], s, E);
-#pragma unroll
-  for (int i = 1; i < K; ++i) {
-    float p, e;
-    ds_prod(a[i], b[i], p, e);
-    const dsf t = ds_two_sum(s, p);
-    s = t.h;
-    E = add_(E, add_(t.l, e));
-  }
-  return ds_two_sum(s, E);
-}
-
 // SloppyDWPlusDW
 GBDW_HD dsf operator+(dsf a, dsf b) {
   using namespace ds_detail;

@@ -80,7 +80,7 @@ struct Elem<GBDW_DS> {
   template <bool SMEM = false>
   __device__ static cpx<dsf> ld(const void* b, int64_t row, int e, int LsP) {
     const double2 a = ldv<SMEM>((const double2*)b + row * LsP + e);
-    return {ds_split_load(a.x), ds_split_load(a.y)};
+    return {ds_split(a.x), ds_split(a.y)};
   }
   __device__ static void st(void* b, int64_t row, int e, int LsP, dsf re, dsf im) {
     ((double2*)b)[row * LsP + e] = make_double2(double(re), double(im));

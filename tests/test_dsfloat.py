@@ -1,6 +1,6 @@
 """The double-word (FP32 pair) arithmetic of the FP64-accurate hopping operator, checked on the
-CPU: the integer splits of FP64 values (exact and load), addition, multiplication, fused
-multiply-add and the compensated dot product against exact results (80-bit long double holds every exact sum / product of the pairs here to
+CPU: the integer split of FP64 values, and addition, multiplication and fused multiply-add
+against exact results (80-bit long double holds every exact sum / product of the pairs here to
 far below the bounds), at the error bounds the header states."""
 import os
 import shutil
@@ -43,37 +43,6 @@ int main() {
     const dsf f = gbdw::fma(a, b, c);
     fma_err = std::fmax(fma_err, (double)(std::fabs(ex(f) - (sa * sb + sc)) / (std::fabs(sa * sb) + std::fabs(sc))));
   }
-  // the load split (unnormalised, |l| < ulp(h)) gives the same value as the exact split, over
-  // the whole exponent range it covers and around its thresholds (2^-74, 2^-126, 2^128)
-  double load_err = 0;
-  int load_bad = 0;
-  for (int i = 0; i < 200000; ++i) {
-    const int ex2 = (i % 7 == 0) ? -75 + (i % 3) : (i % 11 == 0) ? -127 + (i % 3) : (i % 13 == 0) ? 126 + (i % 3)
-                                                                                      : ex_d(rng);
-    const double v = u(rng);
-    const double d = std::ldexp(std::copysign(1.0 + std::fabs(v), v), ex2);
-    const dsf x = gbdw::ds_split_load(d), y = gbdw::ds_split(d);
-    const long double dx = ex(x), dy = ex(y);
-    if (std::isfinite(y.h) && y.h != 0) {
-      load_err = std::fmax(load_err, (double)(std::fabs(dx - dy) / std::fabs((long double)d)));
-      if (std::fabs(x.l) >= std::ldexp(1.0, std::ilogb(x.h) - 23)) ++load_bad;  // |l| < ulp(h)
-    } else if (!(x.h == y.h || (std::isnan(x.h) && std::isnan(y.h)))) {
-      ++load_bad;
-    }
-  }
-  // compensated 6-term dot products against the exact sum, relative to sum |a_i b_i|
-  double dot_err = 0;
-  for (int i = 0; i < 100000; ++i) {
-    dsf a[6], b[6];
-    long double ex_sum = 0, abs_sum = 0;
-    for (int k = 0; k < 6; ++k) {
-      a[k] = dsf(rnd()); b[k] = dsf(rnd());
-      const long double t = ex(a[k]) * ex(b[k]);
-      ex_sum += t; abs_sum += std::fabs(t);
-    }
-    const dsf r = gbdw::ds_dot<6>(a, b);
-    dot_err = std::fmax(dot_err, (double)(std::fabs(ex(r) - ex_sum) / abs_sum));
-  }
   // zero, signs, flushing below 2^-126 and saturation above FP32 range
   const dsf z = dsf(0.0), nz = dsf(-0.0), tiny = dsf(1e-40), big = dsf(1e300), neg = dsf(-3.0);
   // below 2^-74 the trailing part is dropped: 24 bits remain
@@ -82,8 +51,7 @@ int main() {
   const int specials = (z.h == 0 && z.l == 0) + (nz.h == 0 && std::signbit(nz.h)) + (tiny.h == 0) +
                        (std::isinf(big.h) != 0) + (neg.h == -3.0f && neg.l == 0) +
                        (std::fabs((double)sm.h - small) <= 0x1p-23 * small);
-  std::printf("%.3e %.3e %.3e %.3e %d %d %.3e %d %.3e\n", split_err, add_err, mul_err, fma_err, not_normal, specials,
-              load_err, load_bad, dot_err);
+  std::printf("%.3e %.3e %.3e %.3e %d %d\n", split_err, add_err, mul_err, fma_err, not_normal, specials);
   return 0;
 }
 """
@@ -107,7 +75,3 @@ def test_double_word_arithmetic_bounds(tmp_path):
     assert fma_err <= 2.0 ** -45, fma_err
     assert not_normal == 0
     assert specials == 6
-    load_err, load_bad, dot_err = float(out[6]), int(out[7]), float(out[8])
-    assert load_err <= 2.0 ** -47, load_err
-    assert load_bad == 0
-    assert dot_err <= 2.0 ** -45, dot_err
