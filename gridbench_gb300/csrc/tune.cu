@@ -462,7 +462,9 @@ int gbdw_tune_load(const char* path) {
     if (sscanf(key.c_str(), "g%d_s%d_L%d_e%d", &gp, &sp, &LsE, &epi) == 4 &&
         sscanf(text.c_str() + lb, "[%d , %d , %d , %d , %d , %d]", &th, &spt, &mode, &stages, &split, &brick) >= 2 &&
         th > 0 && th <= 256 && th % 32 == 0 && (spt == 1 || spt == 2 || spt == 4) && mode >= 0 && mode <= 4 &&
-        (stages == 2 || stages == 4) && split >= 1 && split <= 64 && brick >= 1 && brick <= 64) {
+        // the double-single keys hold their register cap (CTAs per SM, 3 or 4) in `stages`
+        (stages == 2 || stages == 4 || (epi >= DS_KEY && stages == 3)) && split >= 1 && split <= 64 && brick >= 1 &&
+        brick <= 64) {
       set_tuned_launch(gp, sp, LsE, epi, DhopLaunch{th, spt, mode, stages, split, brick});
       ++loaded;
     }

@@ -150,3 +150,30 @@ def test_fp64_arithmetic_setting_without_a_device():
     assert L.gbdw_tune_set_ds(None, None, 0, 4, 1) == _native.ERR_INVALID
     assert L.gbdw_tune_query_m(None, None, None) == _native.ERR_INVALID
     assert L.gbdw_tune_query_cg(None, None, gb.F64, None) == _native.ERR_INVALID
+
+
+def test_tune_cache_file_round_trip_without_a_device(tmp_path):
+    """The tune cache file is host state: entries of every key family (hopping term, M, the
+    fused CG step, even-odd, double-single with its register cap in `stages`) load and save back
+    unchanged; malformed entries are skipped."""
+    import json
+    entries = {
+        "g1_s1_L16_e0": [64, 2, 2, 2, 1, 1],
+        "g1_s1_L16_e1": [64, 2, 3, 4, 1, 8],
+        "g1_s1_L16_e16": [64, 2, 2, 2, 1, 1],      # CG step, FP64 residual
+        "g2_s2_L16_e33": [64, 2, 3, 4, 1, 1],      # even-odd Schur epilogue (FP16)
+        "g0_s0_L16_e64": [128, 1, 0, 4, 1, 4],     # double-single Dhop, 4 CTAs/SM, t-bricks of 4
+        "g0_s0_L16_e65": [128, 1, 0, 3, 1, 4],     # double-single M, 3 CTAs/SM
+    }
+    bad = {"g1_s1_L12_e0": [100, 2, 0, 4, 1, 1], "g1_s1_L12_e1": [64, 3, 0, 4, 1, 1],
+           "g1_s1_L12_e2": [64, 2, 0, 3, 1, 1]}   # threads, slices and stages out of range
+    src = tmp_path / "in.json"
+    src.write_text(json.dumps({**entries, **bad}))
+    gb.tune_load(str(src))
+    out = tmp_path / "out.json"
+    gb.tune_save(str(out))
+    saved = json.loads(out.read_text())
+    for k, v in entries.items():
+        assert saved.get(k) == v, k
+    for k in bad:
+        assert k not in saved, k
