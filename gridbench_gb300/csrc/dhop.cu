@@ -180,7 +180,8 @@ int run_dhop(const gbdw_gauge* g, gbdw_field* out, const gbdw_field* in, int dag
   }
   int st;
   if (in->prec == GBDW_F64 && g->prec == GBDW_F64 && epi <= 1 && !p.mob && fp64_double_single()) {
-    // double-single arithmetic on the FP64 fields: direct form, its own fixed shape
+    // double-single arithmetic on the FP64 fields: direct form, one slice per thread, with its own
+    // tuned register cap and t-brick order
     if (int s2 = ds_links(g, &p.U)) return s2;
     DhopLaunch D{DS_THREADS, 1, 0, 4};  // stages: register cap as CTAs per SM
     find_tuned_launch(g->prec, in->prec, in->LsE, tune_epi + DS_KEY, &D);
