@@ -337,6 +337,10 @@ int gbdw_tune_query_ds(const gbdw_gauge* g, const gbdw_field* in, int epi, int c
 
 int gbdw_tune_set_ds(const gbdw_gauge* g, const gbdw_field* in, int epi, int minb, int brick) {
   if (!g || !in || epi < 0 || epi > 1 || (minb != 3 && minb != 4) || brick < 1) return GBDW_ERR_INVALID;
+  if (g->prec != GBDW_F64 || in->prec != GBDW_F64) {
+    set_error("gbdw_tune_set_ds: the double-single form runs on F64 gauge and spinor fields");
+    return GBDW_ERR_INVALID;
+  }
   const DhopLaunch L{DS_THREADS, 1, 0, minb, 1, brick};
   if (brick > 1 && brick_extent(g->lat, L) == 0) {
     set_error("gbdw_tune_set_ds: a t-brick needs a periodic lattice whose Lt it divides");

@@ -79,6 +79,9 @@ def test_ds_register_caps_and_t_bricks(ds_ops, minb, brick):
     assert rel_err(y.numpy(), oracle.dwf_m(c["U"], c["phi"], c["nbr"], c["nsite"], Ls, M5, MF, 0)) < TOL
     with pytest.raises(gb.GbdwError):
         gb.tune_set_ds(g, x, 0, 4, 3)  # Lt = 8 is no multiple of 3
+    g32, x32 = gb.Gauge(lat, c["U"], gb.F32), gb.Field(lat, gb.F32)
+    with pytest.raises(gb.GbdwError):
+        gb.tune_set_ds(g32, x32, 0, 4, 1)  # FP32 fields have no double-single form
 
 
 def test_ds_multi_rhs(ds_ops):
