@@ -49,7 +49,7 @@ def test_fp64_16x16_matches_oracle(headline, dag):
 @pytest.mark.parametrize("dag", [0, 1])
 def test_fp32_16x16_matches_oracle_in_every_form(headline, dag):
     """The headline kernel: the tuner's pick and each candidate form, against the FP64
-    oracle at the benchmark spec's 1e-6 relative tolerance."""
+    oracle at the FP32 accuracy target, 1e-6 relative."""
     c, lat, refs = headline
     g = gb.Gauge(lat, c["U"], gb.F32)
     x, y = gb.Field(lat, gb.F32).load(c["phi"]), gb.Field(lat, gb.F32)
